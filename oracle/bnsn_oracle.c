@@ -1,0 +1,2332 @@
+/* bnsn_oracle.c -- CPU oracle for the bns_nurates grey/spectral opacity path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
+ * algorithm (RelNucAs/bns_nurates, include/ headers) used as the checker for the
+ * GPU kernels and as the timed CPU baseline.  The product (the CUDA library in
+ * bns_nurates_gb300/) never links, loads or calls it.
+ *
+ * Each function cites the reference file:line it restates.  Expressions keep
+ * the reference's evaluation order so that, compiled with the same libm and
+ * -ffp-contract=off, results agree bit for bit with the reference built from
+ * its own headers (oracle/_ref, see build_ref.py); the tests check exactly that.
+ *
+ * Data conventions (double, field-major SoA, [field][npts]):
+ *   eos   11 fields: nb temp ye yp yn mu_p mu_n mu_e mu_mu dU dm_eff
+ *   m1    12 fields: n[4] J[4] chi[4]
+ *   distr 28 fields: w_t[4] temp_t[4] eta_t[4] w_f[4] temp_f[4] c_f[4] beta_f[4]
+ *   grey  20 fields: eta_0[4] kappa_0_a[4] eta[4] kappa_a[4] kappa_s[4]
+ *   spec  16 fields of npts*ne: j[4] kappa[4] j_s[4] kappa_s[4] (entry p*ne+e)
+ *   flags  5 ints  : use_abs_em use_pair use_brem use_inelastic_scatt use_iso
+ *   pars   8 ints  : use_dU use_dm_eff use_WM_ab use_WM_sc use_decay
+ *                    brem_impl(0 HR98,1 BRT06,2 GP19) use_NN_medium_corr
+ *                    neglect_blocking
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "bnsn_oracle_consts.h"
+
+#define NSP 4
+#define NMAX 20        /* max quadrature nodes per half-interval */
+#define MMAX (2 * NMAX) /* max energy nodes */
+
+enum { NUE = 0, ANUE = 1, NUX = 2, ANUX = 3 };
+
+typedef struct
+{
+    double nb, temp, ye, yp, yn, mu_p, mu_n, mu_e, mu_mu, dU, dm_eff;
+} eos_t;
+
+typedef struct
+{
+    int use_dU, use_dm_eff, use_WM_ab, use_WM_sc, use_decay, brem_impl,
+        use_NN_medium_corr, neglect_blocking;
+} pars_t;
+
+typedef struct
+{
+    int use_abs_em, use_pair, use_brem, use_inelastic_scatt, use_iso;
+} flags_t;
+
+typedef struct
+{
+    double w_t[NSP], temp_t[NSP], eta_t[NSP];
+    double w_f[NSP], temp_f[NSP], c_f[NSP], beta_f[NSP];
+} distr_t;
+
+typedef struct
+{
+    int n;
+    double x[NMAX], w[NMAX];
+} quad_t;
+
+typedef struct
+{
+    double em[NSP], ab[NSP];
+} kern_t;
+
+/* ===================================================================== */
+/* Special functions (functions.hpp)                                      */
+/* ===================================================================== */
+
+/* functions.hpp:66-75: exp with its argument clamped to [-700, 700]; a NaN
+ * argument maps to the lower bound. */
+static double safe_exp(double x)
+{
+    const double lo = (x > C_EXP_LOW) ? x : C_EXP_LOW;
+    const double cl = (lo < C_EXP_UPP) ? lo : C_EXP_UPP;
+    return exp(cl);
+}
+
+/* Horner evaluation c[0] + t*(c[1] + t*(... + t*c[deg])), innermost first;
+ * the same operation sequence as the nested forms in functions.hpp. */
+static double horner(const double* c, int deg, double t)
+{
+    double p = c[deg];
+    for (int k = deg - 1; k >= 0; --k)
+        p = c[k] + t * p;
+    return p;
+}
+
+/* Complete Fermi-Dirac integrals F_k(y) = int_0^inf x^k/(e^{x-y}+1) dx,
+ * k = 0..5, by the piecewise minimax rational approximations of Fukushima
+ * (Appl. Math. Comput. 259 (2015) 708) as coded in functions.hpp:1550-2838.
+ * Regimes in x = -|y|: x < -2 (series in e^x), -2 <= x <= 0 (rational in
+ * s = -x/2), and y > 0 through the reflection polynomial. NaN gives 0. */
+
+/* functions.hpp:1550-1612 */
+static double fdi_0(double y)
+{
+    static const double an[5] = {22696.2126132366633, 5222.0667923565138,
+                                 357.623326425354522, 6.9167792879948140,
+                                 0.00200096064827815813};
+    static const double ad[5] = {45392.4252264733267, 14539.5980679273792,
+                                 1611.36476693109675, 71.072178562726798, 1.0};
+    static const double bn[9] = {
+        159.601717762460980,    23.7193942338278703,   0.377783268730614356,
+        10.5181677709577503,    3.78181326142271599,   -0.441998676614933572,
+        -0.450072959113928254,  -0.0734798777056723512, 0.000915454570009894267};
+    static const double bd[8] = {284.26032127745967, 315.2592651624449,
+                                 310.2713981221035,  206.21640678892182,
+                                 96.77898293084927,  35.456591489081173,
+                                 8.1762315442738975, 1.0};
+    const double x = -fabs(y);
+    double fd = 0.;
+    if (x < -2.)
+    {
+        const double ex = exp(x);
+        const double t  = ex * C_FDI_LIT;
+        fd = ex * (1. - ex * horner(an, 4, t) / horner(ad, 4, t));
+    }
+    else if (x <= 0.)
+    {
+        const double s = -0.5 * x;
+        const double t = 1. - s;
+        fd = horner(bn, 8, t) / horner(bd, 7, s);
+    }
+    if (y > 0.)
+        fd = fd + y;
+    return fd;
+}
+
+/* functions.hpp:1795-1860 */
+static double fdi_p1(double y)
+{
+    static const double an[5] = {22189.1070807945062, 4915.92700908746777,
+                                 322.901386168881348, 5.9897442965804548,
+                                 0.00397641173774375092};
+    static const double ad[5] = {88756.428323178025, 25002.3197546553836,
+                                 2389.06277237306633, 88.376214553692756, 1.0};
+    static const double bn[9] = {
+        145.488167182330098,  251.392824471576922,  56.6537141912783024,
+        17.9918985363509694,  20.1369115558099802,  7.09659390228556164,
+        0.199701180197912643, -0.403173132925886253, -0.0792966701498222697};
+    static const double bd[9] = {606.0757707716040,   374.1806357435014,
+                                 252.1367051536344,   27.2746245830016,
+                                 -61.57766112137513,  -53.72117554363975,
+                                 -25.678454878692950, -7.1995819520154718,
+                                 -1.0};
+    const double x = -fabs(y);
+    double fd = 0.;
+    if (x < -2.)
+    {
+        const double ex = exp(x);
+        const double t  = ex * C_FDI_LIT;
+        fd = ex * (1. - ex * horner(an, 4, t) / horner(ad, 4, t));
+    }
+    else if (x <= 0.)
+    {
+        const double s = -0.5 * x;
+        const double t = 1. - s;
+        fd = horner(bn, 8, t) / horner(bd, 8, s);
+    }
+    if (y > 0.)
+        fd = -fd + 1.64493406684822644 + 0.5 * y * y;
+    return fd;
+}
+
+/* functions.hpp:2051-2112 */
+static double fdi_p2(double y)
+{
+    static const double an[4] = {1914.06748184935743, 273.085756700981399,
+                                 8.5861610217850095, 0.0161890243763741414};
+    static const double ad[4] = {7656.2699273974454, 1399.35442210906621,
+                                 72.929152915475392, 1.0};
+    static const double bn[9] = {
+        2711.49678259128843,  1299.85460914884154, 222.606134197895041,
+        172.881855215582924,  112.951038040682055, 24.0376482128898634,
+        -2.68393549333878715, -2.14077421411719935, -0.326188299771397236};
+    static const double bd[9] = {2517.1726659917047, 3038.7689794575778,
+                                 2541.7823512372631, 1428.0589853413436,
+                                 531.62378035996132, 122.54595216479181,
+                                 8.395768655115050,  -3.9142702096919080,
+                                 -1.0};
+    const double x = -fabs(y);
+    double fd = 0.;
+    if (x < -2.)
+    {
+        const double ex = exp(x);
+        const double t  = ex * C_FDI_LIT;
+        fd = ex * (2. - ex * horner(an, 3, t) / horner(ad, 3, t));
+    }
+    else if (x <= 0.)
+    {
+        const double s = -0.5 * x;
+        const double t = 1. - s;
+        fd = horner(bn, 8, t) / horner(bd, 8, s);
+    }
+    if (y > 0.)
+        fd = fd + y * (3.28986813369645287 + 0.333333333333333333 * y * y);
+    return fd;
+}
+
+/* functions.hpp:2293-2350 */
+static double fdi_p3(double y)
+{
+    static const double an[4] = {5121.6401850302408, 664.28706260743472,
+                                 19.0856927562699544, 0.0410982603688952131};
+    static const double ad[4] = {13657.7071600806539, 2136.54222460571183,
+                                 92.376788603062645, 1.0};
+    static const double bn[8] = {7881.24597452900838, 4323.07526636309661,
+                                 1260.13125873282465, 653.359212389160499,
+                                 354.630774329461644, 113.373708671587772,
+                                 19.9559488532742796, 1.59407954898394322};
+    static const double bd[8] = {2570.7250703533430, 2972.7443644211129,
+                                 2393.9995533270879, 1259.0724833462608,
+                                 459.86413596901097, 112.60906419590854,
+                                 16.468882811659000, 1.0};
+    const double x = -fabs(y);
+    double fd = 0.;
+    if (x < -2.)
+    {
+        const double ex = exp(x);
+        const double t  = ex * C_FDI_LIT;
+        fd = ex * (6. - ex * horner(an, 3, t) / horner(ad, 3, t));
+    }
+    else if (x <= 0.)
+    {
+        const double s = -0.5 * x;
+        const double t = 1. - s;
+        fd = horner(bn, 7, t) / horner(bd, 7, s);
+    }
+    if (y > 0.)
+    {
+        const double y2 = y * y;
+        fd = -fd + 11.3643939539669510 + y2 * (4.93480220054467931 + y2 * 0.25);
+    }
+    return fd;
+}
+
+/* functions.hpp:2535-2592 */
+static double fdi_p4(double y)
+{
+    static const double an[4] = {18247.2542465629199, 2120.56302902849207,
+                                 54.659507299984584, 0.121876197098273914};
+    static const double ad[4] = {24329.6723287505678, 3261.01909656925521,
+                                 117.071576489684022, 1.0};
+    static const double bn[8] = {33093.9102025608137, 19031.4783357798975,
+                                 5431.08357152245897, 2393.94262931609398,
+                                 1268.40017257978070, 418.662172475927160,
+                                 77.4108960876508190, 6.67374311450268357};
+    static const double bd[8] = {2645.4885670047153, 3236.2237702166948,
+                                 2500.5977847175497, 1278.0109577275445,
+                                 448.99020896813485, 105.86020755838874,
+                                 15.216887271751039, 1.0};
+    const double x = -fabs(y);
+    double fd = 0.;
+    if (x < -2.)
+    {
+        const double ex = exp(x);
+        const double t  = ex * C_FDI_LIT;
+        fd = ex * (24. - ex * horner(an, 3, t) / horner(ad, 3, t));
+    }
+    else if (x <= 0.)
+    {
+        const double s = -0.5 * x;
+        const double t = 1. - s;
+        fd = horner(bn, 7, t) / horner(bd, 7, s);
+    }
+    if (y > 0.)
+    {
+        const double y2 = y * y;
+        fd = fd + y * (45.4575758158678040 +
+                       y2 * (6.57973626739290575 + y2 * 0.2));
+    }
+    return fd;
+}
+
+/* functions.hpp:2778-2838 */
+static double fdi_p5(double y)
+{
+    static const double an[4] = {81190.938912603315, 8368.4990332049831,
+                                 190.753830813273698, 0.413800735538960261};
+    static const double ad[4] = {43301.8340867217726, 4977.68099709243407,
+                                 148.484432990224213, 1.0};
+    static const double bn[8] = {159651.547840031111, 96307.2005742063042,
+                                 26923.5693307648389, 9274.54751848368696,
+                                 4445.76333033698006, 1461.45267097859337,
+                                 272.164427980501432, 23.6526046298891619};
+    static const double bd[8] = {2522.7839609396783, 3244.5527999477567,
+                                 2403.0532924519756, 1176.7202478443275,
+                                 397.7596246691212,  91.84661231161838,
+                                 13.491911254479298, 1.0};
+    const double x = -fabs(y);
+    double fd = 0.;
+    if (x < -2.)
+    {
+        const double ex = exp(x);
+        const double t  = ex * C_FDI_LIT;
+        fd = ex * (120. - ex * horner(an, 3, t) / horner(ad, 3, t));
+    }
+    else if (x <= 0.)
+    {
+        const double s = -0.5 * x;
+        const double t = 1. - s;
+        fd = horner(bn, 7, t) / horner(bd, 7, s);
+    }
+    if (y > 0.)
+    {
+        const double y2 = y * y;
+        fd = -fd + 236.532261911384425 +
+             y2 * (113.643939539669510 +
+                   y2 * (8.22467033424113218 + y2 * 0.166666666666666667));
+    }
+    return fd;
+}
+
+/* functions.hpp:4376-4396: Fermi-Dirac occupation, split on the sign of
+ * the exponent so exp never overflows. */
+static double fermi_distr(double e, double temp, double mu)
+{
+    const double arg = (e - mu) / temp;
+    if (arg > 0.)
+    {
+        const double tmp = safe_exp(-arg);
+        return tmp / (tmp + 1.);
+    }
+    const double tmp = safe_exp(arg);
+    return 1. / (tmp + 1.);
+}
+
+/* functions.hpp:4401-4413: the e^x-dependent denominator factor of the NES
+ * kernel: 1/(1-e^{-x}) for x < 0 and -e^{-x}/(1-e^{-x}) for x >= 0, with the
+ * x == 0 singularity guarded. */
+static double neps_exp_func(double x)
+{
+    const double ex  = safe_exp(-fabs(x));
+    const int is_neg = signbit(x) != 0;
+    return (is_neg - (!is_neg) * ex) / (1. - ex + (x == 0.));
+}
+
+/* functions.hpp:99-137: modified Bessel I1 (polynomial fits) */
+static double bessi1(double x)
+{
+    static const double a[7] = {0.5,          0.87890594,  0.51498869,
+                                0.15084934,   0.2658733e-1, 0.301532e-2,
+                                0.32411e-3};
+    static const double b[9] = {0.2282967e-1, -0.2895312e-1, 0.1787654e-1,
+                                0.420059e-2,  0.39894228,    -0.3988024e-1,
+                                -0.362018e-2, 0.163801e-2,   -0.1031555e-1};
+    double ax, ans, y;
+    if ((ax = fabs(x)) < 3.75)
+    {
+        y   = x / 3.75;
+        y   = y * y;
+        ans = ax * (a[0] +
+                    y * (a[1] + y * (a[2] + y * (a[3] + y * (a[4] +
+                                                             y * (a[5] + y * a[6]))))));
+    }
+    else
+    {
+        y   = 3.75 / ax;
+        ans = b[0] + y * (b[1] + y * (b[2] - y * b[3]));
+        ans = b[4] + y * (b[5] + y * (b[6] + y * (b[7] + y * (b[8] + y * ans))));
+        ans *= (exp(ax) / sqrt(ax));
+    }
+    return x < 0. ? -ans : ans;
+}
+
+/* functions.hpp:140-180: modified Bessel K1 (polynomial fits) */
+static double bessk1(double x)
+{
+    static const double a[8] = {1.0,          1.0,          0.15443144,
+                                -0.67278579,  -0.18156897,  -0.1919402e-1,
+                                -0.110404e-2, -0.4686e-4};
+    static const double b[7] = {1.25331414,   0.23498619,   -0.3655620e-1,
+                                0.1504268e-1, -0.780353e-2, 0.325614e-2,
+                                -0.68245e-3};
+    double y, ans;
+    if (x <= 2.)
+    {
+        y   = x * x / 4.;
+        ans = (log(x / 2.) * bessi1(x)) +
+              (a[0] / x) *
+                  (a[1] +
+                   y * (a[2] +
+                        y * (a[3] + y * (a[4] + y * (a[5] + y * (a[6] + y * (a[7])))))));
+    }
+    else
+    {
+        y   = 2. / x;
+        ans = (exp(-x) / sqrt(x)) *
+              (b[0] +
+               y * (b[1] + y * (b[2] + y * (b[3] + y * (b[4] + y * (b[5] + y * (b[6])))))));
+    }
+    return ans;
+}
+
+/* functions.hpp:4460-4471 */
+static double gamma_stirling(double x)
+{
+    return sqrt(6.283185307179586 / x) * pow(x / 2.718281828459045235360287471352, x);
+}
+
+/* ===================================================================== */
+/* Distribution reconstruction (distribution.hpp)                          */
+/* ===================================================================== */
+
+/* distribution.hpp:51-175: optically thick (Fermi-Dirac) parameters from the
+ * number and energy densities: eta_t from a piecewise rational fit of
+ * y = n (n/J)^3 / (4 pi/(hc)^3), capped at 20; T_t = F2(eta) J / (F3(eta) n). */
+static void thick_params(const double* n_in, const double* J_in,
+                         const double* chi_in, distr_t* d)
+{
+    static const double nu1[6] = {0.19926987701997, 38865.0149220478,
+                                  14364.6331099737, 5750.1878570758,
+                                  1120.71610972194, 1.60356108438235e-8};
+    static const double nu2[7] = {41.3836568203438,  32.5515666786612,
+                                  157.774993512235,  66.5726772426253,
+                                  14.4883415579211,  0.315360380575709,
+                                  0.000660414331285249};
+    static const double nu3[7] = {3852.81416018959,    5316.18895799799,
+                                  1102.91561586553,    1.54082262710661e-6,
+                                  1732.89925128741,    1769.59868329086,
+                                  586.406885304906};
+    static const double de1[6] = {1.0,              38840.0743174942,
+                                  99.9009680656931, 171.874844843596,
+                                  75.7101579899442, 83.0160130941424};
+    static const double de2[6] = {1.8888797407042,   5.35488690539183,
+                                  1.94673781342617,  0.483128792035557,
+                                  0.0113386564109086, 2.64160073447322e-5};
+    static const double de3[6] = {255.936658313629, 9.42360945627147e-5,
+                                  81.2467063138386, 180.100197053091,
+                                  89.0343496217014, 143.849128123195};
+    for (int s = 0; s < NSP; ++s)
+    {
+        const double n   = (n_in[s] > 1e-100) ? n_in[s] : 1e-100;
+        const double J   = (J_in[s] > 1e-100) ? J_in[s] : 1e-100;
+        const double chi = chi_in[s];
+        d->w_t[s]        = 1.5 * (1. - chi);
+        const double q   = n / J;
+        const double y   = n * (q * q * q) / C_FOURPI_HC3;
+        double eta;
+        if (y < 0.005)
+        {
+            const double num =
+                y * (y * (y * (y * (y * (y + nu1[0]) + nu1[1]) + nu1[2]) + nu1[3]) +
+                     nu1[4]) +
+                nu1[5];
+            const double den =
+                y * (y * (y * (y * (y * (y + de1[0]) + de1[1]) - de1[2]) - de1[3]) +
+                     de1[4]) +
+                de1[5];
+            eta = log(num / den);
+        }
+        else if (y <= 0.7)
+        {
+            const double num =
+                y * (y * (y * (y * (y * (nu2[0] * y + nu2[1]) - nu2[2]) + nu2[3]) +
+                          nu2[4]) +
+                     nu2[5]) +
+                nu2[6];
+            const double den =
+                y * (y * (y * (y * (y * (y + de2[0]) - de2[1]) + de2[2]) + de2[3]) +
+                     de2[4]) +
+                de2[5];
+            eta = num / den - 30.;
+        }
+        else if (y > 0.7 && y < 0.7901234567745267)
+        {
+            const double num =
+                y * (y * (y * (y * (y * (nu3[0] * y - nu3[1]) + nu3[2]) + nu3[3]) +
+                          nu3[4]) -
+                     nu3[5]) +
+                nu3[6];
+            const double den =
+                y * (y * (y * (y * (y * (y + de3[0]) + de3[1]) - de3[2]) - de3[3]) -
+                     de3[4]) +
+                de3[5];
+            eta = exp(num / den);
+        }
+        else
+        {
+            eta = 20.;
+        }
+        eta          = (eta < 20.) ? eta : 20.;
+        d->eta_t[s]  = eta;
+        d->temp_t[s] = fdi_p2(eta) * J / (fdi_p3(eta) * n);
+    }
+}
+
+/* distribution.hpp:206-243: optically thin (power-law Maxwellian) part with
+ * c_f = 0.6: T_f = J/(n (c_f+3)), beta_f = n/(4pi/(hc)^3 Gamma(c_f+3) T_f^(c_f+3)). */
+static void thin_params(const double* n_in, const double* J_in,
+                        const double* chi_in, distr_t* d)
+{
+    const double c_f = 0.6;
+    for (int s = 0; s < NSP; ++s)
+    {
+        const double n   = (n_in[s] > 1e-100) ? n_in[s] : 1e-100;
+        const double J   = (J_in[s] > 1e-100) ? J_in[s] : 1e-100;
+        const double chi = chi_in[s];
+        d->w_f[s]        = 0.5 * (3. * chi - 1.);
+        d->c_f[s]        = c_f;
+        const double Tnu = J / (n * (c_f + 3.));
+        d->temp_f[s]     = Tnu;
+        d->beta_f[s] =
+            n / (C_FOURPI_HC3 * gamma_stirling(c_f + 3.) * pow(Tnu, c_f + 3.));
+    }
+}
+
+/* distribution.hpp:323-333 */
+static void distr_from_m1(const double* n, const double* J, const double* chi,
+                          distr_t* d)
+{
+    thick_params(n, J, chi, d);
+    thin_params(n, J, chi, d);
+}
+
+/* distribution.hpp:253-290 */
+static void nu_equilibrium(const eos_t* e, distr_t* d)
+{
+    const double T = e->temp;
+    for (int s = 0; s < NSP; ++s)
+    {
+        d->w_t[s]    = 1.;
+        d->temp_t[s] = T;
+        d->w_f[s]    = 0.;
+        d->c_f[s]    = 0.6;
+        d->temp_f[s] = T;
+        d->beta_f[s] = 1.;
+    }
+    d->eta_t[NUE]  = (e->mu_e - e->mu_n + e->mu_p) / T;
+    d->eta_t[ANUE] = -d->eta_t[NUE];
+    d->eta_t[NUX]  = 0.;
+    d->eta_t[ANUX] = 0.;
+}
+
+/* distribution.hpp:298-315 with NuFThick :31-38 and NuFThin :186-195 */
+static double total_nu_f(double omega, const distr_t* d, int s)
+{
+    const double T_t    = d->temp_t[s];
+    const double f_thick = fermi_distr(omega, T_t, d->temp_t[s] * d->eta_t[s]);
+    const double f_thin =
+        d->beta_f[s] * pow(omega, d->c_f[s]) * exp(-omega / d->temp_f[s]);
+    return d->w_t[s] * f_thick + d->w_f[s] * f_thin;
+}
+
+/* ===================================================================== */
+/* Weak magnetism (weak_magnetism.hpp)                                     */
+/* ===================================================================== */
+
+/* weak_magnetism.hpp:45-104: single-nucleon form factors (Horowitz 2002);
+ * reac 1: scattering on protons, 2: on neutrons, 3: charged-current. */
+static void nuc_form_factors(double E, int reac, double* cv, double* ca,
+                             double* F2)
+{
+    const double lamp = 1.793, lamn = -1.913;
+    const double ehor = E * C_WM_ESCALE;
+    const double tau  = 0.5 * SQ(ehor) / (1. + ehor);
+    const double eta  = 1. / (1. + 5.6 * tau);
+    const double G    = 1. / pow(1. + 4.97 * tau, 2.);
+    const double Fp1  = (1. + tau * (1. + lamp)) * G / (1. + tau);
+    const double Fp2  = lamp * G / (1. + tau);
+    const double Fn1  = tau * lamn * (1. - eta) * G / (1. + tau);
+    const double Fn2  = lamn * (1. + tau * eta) * G / (1. + tau);
+    const double d3   = 1. + 3.53 * tau;
+    if (reac == 1)
+    {
+        *cv = (0.5 - 2. * C_SINTHW2) * Fp1 - 0.5 * Fn1;
+        *ca = 0.5 * (C_GA - C_GS) / SQ(d3);
+        *F2 = (0.5 - 2. * C_SINTHW2) * Fp2 - 0.5 * Fn2;
+    }
+    else if (reac == 2)
+    {
+        *cv = (0.5 - 2. * C_SINTHW2) * Fn1 - 0.5 * Fp1;
+        *ca = -0.5 * (C_GA + C_GS) / SQ(d3);
+        *F2 = (0.5 - 2. * C_SINTHW2) * Fn2 - 0.5 * Fp2;
+    }
+    else
+    {
+        *cv = Fp1 - Fn1;
+        *ca = C_GA / SQ(d3);
+        *F2 = Fp2 - Fn2;
+    }
+}
+
+/* weak_magnetism.hpp:123-160: recoil/WM correction of the beta rates */
+static void wm_abs_em(double omega, double* R, double* Rbar)
+{
+    double cv, ca, F2;
+    nuc_form_factors(omega, 3, &cv, &ca, &F2);
+    const double e    = omega * C_WM_ESCALE;
+    const double tmp1 = SQ(cv) * (1. + 4. * e + (16. / 3.) * SQ(e)) +
+                        3. * ca * ca * SQ(1. + (4. / 3.) * e) +
+                        (8. / 3.) * cv * F2 * SQ(e) +
+                        (5. / 3.) * SQ(e) * (1. + (2. / 5.) * e) * SQ(F2);
+    const double tmp2 = 4. * (cv + F2) * ca * e * (1. + (4. / 3.) * e);
+    const double tmp3 = (SQ(C_GV) + 3. * SQ(C_GA)) * CUBE(1. + 2. * e);
+    *R    = (tmp1 + tmp2) / tmp3;
+    *Rbar = (tmp1 - tmp2) / tmp3;
+}
+
+/* weak_magnetism.hpp:165-210: WM correction of the l = 0, 1 scattering
+ * Legendre coefficients */
+static void wm_scatt(double omega, int reac, double* R0, double* R1)
+{
+    double cv, ca, F2, h0, h1;
+    nuc_form_factors(omega, reac, &cv, &ca, &F2);
+    if (reac == 1)
+    {
+        h0 = SQ(C_HPV) + 3. * SQ(C_HPA);
+        h1 = SQ(C_HPV) - SQ(C_HPA);
+    }
+    else
+    {
+        h0 = SQ(C_HNV) + 3. * SQ(C_HNA);
+        h1 = SQ(C_HNV) - SQ(C_HNA);
+    }
+    const double e = omega * C_WM_ESCALE;
+    *R0 = (SQ(cv) + 3. * SQ(ca) + 1.5 * SQ(e * F2) + 2. * SQ(e) * cv * F2) / h0;
+    *R1 = (SQ(cv) - SQ(ca) - 2. * SQ(e * F2) - 4. * SQ(e) * cv * F2) / h1;
+}
+
+/* ===================================================================== */
+/* Beta processes (formulas_beta_iso.hpp:64-341)                           */
+/* ===================================================================== */
+
+/* formulas_beta_iso.hpp:64-97 (Bruenn C14) */
+static double eta_nn_abs(double n_in, double n_out, double mu_hat, double T)
+{
+    if (fabs(mu_hat) < 1.0e-02)
+        return n_in;
+    const double etanp = (n_out - n_in) / (safe_exp(-mu_hat / T) - 1.);
+    if (etanp < 0.)
+        return n_in;
+    return etanp;
+}
+
+/* formulas_beta_iso.hpp:138-279: out[0] = abs nu, out[1] = em nu,
+ * out[2] = abs anti-nu, out[3] = em anti-nu [s^-1]; absorption from detailed
+ * balance. */
+static void abs_opacity_single_lep(double omega, const pars_t* p,
+                                   const eos_t* eos, double m_l, double mu_l,
+                                   double* out)
+{
+    const double m2 = SQ(m_l);
+    double cap = 0., dec = 0., R = 1., Rbar = 1., dU = 0., dQ = C_Q;
+    const double T  = eos->temp;
+    const double nn = eos->nb * eos->yn;
+    const double np = eos->nb * eos->yp;
+    if (p->use_dU)
+        dU = eos->dU;
+    if (p->use_dm_eff)
+        dQ = eos->dm_eff;
+    const double mu_hat = eos->mu_n - eos->mu_p - dQ;
+    const double Qprime = dQ + dU;
+    const double mu_np  = mu_hat - dU;
+    const double etanp  = eta_nn_abs(nn, np, mu_np, T);
+    const double etapn  = eta_nn_abs(np, nn, -mu_np, T);
+    if (p->use_WM_ab)
+        wm_abs_em(omega, &R, &Rbar);
+
+    double Ee = omega + Qprime, Ep = -Ee;
+    double Ee2 = Ee * Ee, Ep2 = Ep * Ep;
+    double fe = fermi_distr(Ee, T, +mu_l);
+    double fp = fermi_distr(Ep, T, -mu_l);
+    if (Ee - m_l >= 0.)
+        cap = Ee2 * sqrt(1. - m2 / Ee2) * R;
+    if (p->use_decay && Ep - m_l >= 0.)
+        dec = Ep2 * sqrt(1. - m2 / Ep2);
+    out[1] = C_BETA_CONST * etapn * (cap * fe + dec * (1. - fp));
+    out[0] = out[1] * safe_exp((omega - (eos->mu_p + mu_l - eos->mu_n)) / T);
+
+    cap = 0.;
+    dec = 0.;
+    Ep  = omega - Qprime;
+    Ee  = -Ep;
+    Ee2 = Ee * Ee;
+    Ep2 = Ep * Ep;
+    fe  = fermi_distr(Ee, T, +mu_l);
+    fp  = fermi_distr(Ep, T, -mu_l);
+    if (Ep - m_l >= 0.)
+        cap = Ep2 * sqrt(1. - m2 / Ep2) * Rbar;
+    if (p->use_decay && Ee - m_l >= 0.)
+        dec = Ee2 * sqrt(1. - m2 / Ee2);
+    out[3] = C_BETA_CONST * etanp * (cap * fp + dec * (1. - fe));
+    out[2] = out[3] * safe_exp((omega - (eos->mu_n - eos->mu_p - mu_l)) / T);
+}
+
+/* formulas_beta_iso.hpp:291-341: AbsOpacity / StimAbsOpacity for electrons.
+ * out[4] = abs_nue, em_nue, abs_anue, em_anue. */
+static void abs_opacity(double omega, const pars_t* p, const eos_t* eos,
+                        int stimulated, double* out)
+{
+    double o[4] = {0., 0., 0., 0.};
+    abs_opacity_single_lep(omega, p, eos, C_ME, eos->mu_e, o);
+    out[0] = o[0];
+    out[1] = o[1];
+    out[2] = o[2];
+    out[3] = o[3];
+    if (stimulated)
+    {
+        out[0] = out[0] + out[1];
+        out[2] = out[2] + out[3];
+    }
+}
+
+/* ===================================================================== */
+/* Iso-energetic scattering on nucleons (formulas_beta_iso.hpp:371-564)    */
+/* ===================================================================== */
+
+/* formulas_beta_iso.hpp:371-395 (Bruenn C37) */
+static double eta_nn_sc(double nb, double temp, double yN)
+{
+    const double nN = yN * nb;
+    if (nN <= 0.)
+        return 0.;
+    const double eFN = C_ISO_EF * pow(nN, 2. / 3.);
+    const double aux = 1.5 * temp / eFN;
+    return nN * aux / sqrt(1. + SQ(aux));
+}
+
+/* formulas_beta_iso.hpp:411-451 */
+static double iso_scatt_nucleon(double omega, const pars_t* p, const eos_t* eos,
+                                double yN, int reac)
+{
+    double R0 = 1., R1 = 1., leg0, leg1;
+    const double etaNN = eta_nn_sc(eos->nb, eos->temp, yN);
+    if (p->use_WM_sc)
+        wm_scatt(omega, reac, &R0, &R1);
+    if (reac == 1)
+    {
+        leg0 = C_ISO_C0P * R0;
+        leg1 = C_ISO_C1P * R1;
+    }
+    else
+    {
+        leg0 = C_ISO_C0N * R0;
+        leg1 = C_ISO_C1N * R1;
+    }
+    return etaNN * (leg0 - leg1 / 3.);
+}
+
+/* formulas_beta_iso.hpp:497-507 */
+static double iso_scatt_total(double omega, const pars_t* p, const eos_t* eos)
+{
+    const double pr = iso_scatt_nucleon(omega, p, eos, eos->yp, 1);
+    const double ne = iso_scatt_nucleon(omega, p, eos, eos->yn, 2);
+    return pr + ne;
+}
+
+/* formulas_beta_iso.hpp:523-564 */
+static double iso_scatt_leg_coeff(double omega, const pars_t* p,
+                                  const eos_t* eos, int l)
+{
+    double R0p = 1., R1p = 1., R0n = 1., R1n = 1.;
+    const double eta_pp = eta_nn_sc(eos->nb, eos->temp, eos->yp);
+    const double eta_nn = eta_nn_sc(eos->nb, eos->temp, eos->yn);
+    if (p->use_WM_sc)
+    {
+        wm_scatt(omega, 1, &R0p, &R1p);
+        wm_scatt(omega, 2, &R0n, &R1n);
+    }
+    if (l == 0)
+        return eta_pp * C_ISO_C0P * R0p + eta_nn * C_ISO_C0N * R0n;
+    return eta_pp * C_ISO_C1P * R1p + eta_nn * C_ISO_C1N * R1n;
+}
+
+/* ===================================================================== */
+/* e+e- pair annihilation kernel (kernel_pair.hpp)                         */
+/* ===================================================================== */
+
+/* kernel_pair.hpp:16-120: Pons et al. (1998) Psi_0(y,z) and Psi_0(z,y) as
+ * polynomials in y, z over complete FD integrals at eta, eta+-y, eta+-z and
+ * eta+-(y+z); suppressed to 0 when eta - y - z > 200. */
+static void pair_psi(double y, double z, double eta, double* psi)
+{
+    if (eta - y - z > 200.)
+    {
+        psi[0] = 0.;
+        psi[1] = 0.;
+        return;
+    }
+    const double a1my = fdi_p1(eta - y), a1mz = fdi_p1(eta - z);
+    const double a1py = fdi_p1(eta + y), a1pz = fdi_p1(eta + z);
+    const double a2my = fdi_p2(eta - y), a2mz = fdi_p2(eta - z);
+    const double a2py = fdi_p2(eta + y), a2pz = fdi_p2(eta + z);
+    const double a3e = fdi_p3(eta);
+    const double a3my = fdi_p3(eta - y), a3mz = fdi_p3(eta - z);
+    const double a3py = fdi_p3(eta + y), a3pz = fdi_p3(eta + z);
+    const double a3myz = fdi_p3(eta - y - z), a3pyz = fdi_p3(eta + y + z);
+    const double a4e = fdi_p4(eta);
+    const double a4my = fdi_p4(eta - y), a4mz = fdi_p4(eta - z);
+    const double a4py = fdi_p4(eta + y), a4pz = fdi_p4(eta + z);
+    const double a4myz = fdi_p4(eta - y - z), a4pyz = fdi_p4(eta + y + z);
+    const double a5my = fdi_p5(eta - y), a5mz = fdi_p5(eta - z);
+    const double a5py = fdi_p5(eta + y), a5pz = fdi_p5(eta + z);
+    const double a5myz = fdi_p5(eta - y - z), a5pyz = fdi_p5(eta + y + z);
+
+    const double c0  = 20. * a4my;
+    const double c1  = 20. * a4pz;
+    const double c2  = 120. * a2my - 120. * a2pz;
+    const double c3  = -40. * a3my + 40. * a3pz;
+    const double c4  = 40. * a3e;
+    const double c5  = 40. * a3myz - c4;
+    const double c6  = -20. * a4e;
+    const double c7  = 20. * a4myz + c6;
+    const double c8  = -40. * a3pyz + c4;
+    const double c9  = 20. * a4pyz + c6;
+    const double c10 = -4. * a5my + 4. * a5myz - 4. * a5mz + 4. * a5py -
+                       4. * a5pyz + 4. * a5pz;
+    const double c11 = 20. * a4py;
+    const double c12 = 20. * a4mz;
+    const double c13 = -40. * a3mz + 40. * a3py;
+    const double c14 = 120. * a2mz - 120. * a2py;
+    const double den = 15. * SQ(y * z);
+
+    double p0 =
+        c10 +
+        y * (-c0 + c1 + c7 + y * (c3 + c5 + z * (c2 + z * (-120. * a1my + 120. * a1pz))) +
+             z * (80. * a3my - 80. * a3pz - c2 * z)) +
+        z * (c0 - c1 + c9 + z * (c3 + c8));
+    double p1 =
+        c10 + y * (-c11 + c12 + c9 + y * (c13 + c8)) +
+        z * (c11 - c12 + c7 + y * (80. * a3mz - 80. * a3py - c14 * y) +
+             z * (c13 + c5 + y * (c14 + y * (-120. * a1mz + 120. * a1py))));
+    psi[0] = p0 / den;
+    psi[1] = p1 / den;
+}
+
+/* kernel_pair.hpp:135-198: production kernel em = Phi/2 per species and the
+ * annihilation kernel abs = e^{(w+w')/T} em. */
+static void pair_kernels(double temp, double mu_e, double omega,
+                         double omega_prime, kern_t* k)
+{
+    const double T   = temp;
+    const double eta = mu_e / T;
+    const double y   = omega / T;
+    const double z   = omega_prime / T;
+    const double aux = C_PAIR_PHI * SQ(T) / (1. - safe_exp(y + z));
+    double psi[2];
+    pair_psi(y, z, eta, psi);
+    double phi[4];
+    phi[0] = (SQ(C_PAIR_A1E) * psi[0] + SQ(C_PAIR_A2E) * psi[1]) * aux;
+    phi[1] = (SQ(C_PAIR_A1E) * psi[1] + SQ(C_PAIR_A2E) * psi[0]) * aux;
+    phi[2] = (SQ(C_PAIR_A1X) * psi[0] + SQ(C_PAIR_A2X) * psi[1]) * aux;
+    phi[3] = (SQ(C_PAIR_A1X) * psi[1] + SQ(C_PAIR_A2X) * psi[0]) * aux;
+    for (int s = 0; s < NSP; ++s)
+        k->em[s] = 0.5 * phi[s];
+    for (int s = 0; s < NSP; ++s)
+        k->ab[s] = safe_exp((omega + omega_prime) / T) * k->em[s];
+}
+
+/* ===================================================================== */
+/* NN bremsstrahlung: HR98 (kernel_brem_HR98.hpp)                           */
+/* ===================================================================== */
+
+/* kernel_brem_HR98.hpp:33-152: s-component fit, Hannestad & Raffelt Eq.(49) */
+static double hr98_s(double x, double y, double eta_star)
+{
+    x        = (x > C_BREM_XMIN) ? x : C_BREM_XMIN;
+    y        = (y > C_BREM_YMIN) ? y : C_BREM_YMIN;
+    eta_star = (eta_star > C_BREM_ETAMIN) ? eta_star : C_BREM_ETAMIN;
+
+    const double snd_num = 2. * C_SQRTPI * pow(x + 2. - safe_exp(-y / 12.), 1.5) *
+                           (SQ(x) + 2. * x * y + 5. * SQ(y) / 3. + 1.);
+    const double q       = C_PI_1_8 + x + y;
+    const double snd_den = C_SQRTPI + q * q * q * q;
+    const double s_nd    = snd_num / snd_den;
+
+    const double u    = sqrt(y / (2. * eta_star)) + 1.e-10;
+    const double u2   = SQ(u);
+    const double uarg = u2 / (2. * sqrt(2. * u2 + 4.));
+    double f_u        = (1. - 5. * u * atan(2. / u) / 6. + u2 / (3. * (u2 + 4.)) +
+                  atan(1. / uarg) * uarg / 3.);
+    f_u = (fabs(f_u) < 1.e-14) ? 1.e-14 : f_u;
+
+    const double s_d = 3. * C_PIHALF_5_2 * pow(eta_star, -2.5) *
+                       (SQ(x) + C_FOURPISQ) * x * f_u /
+                       (C_FOURPISQ * (1. - safe_exp(-x)));
+    const double px11  = pow(x, 1.1);
+    const double f_den = (3. + SQ(x - 1.2) + pow(x, -4.)) * (1. + SQ(eta_star)) *
+                         (1. + y * y * y * y);
+    const double f_brem = 1. + 1. / f_den;
+    const double g_brem = 1. - 0.0044 * px11 * y / (0.8 + 0.06 * pow(y, 1.05)) *
+                                   sqrt(eta_star) / (eta_star + 0.2);
+    const double h_brem = 0.1 * eta_star / (2.39 + 0.1 * pow(eta_star, 1.1));
+    const double c_brem = 1.1 * px11 * h_brem /
+                          (2.3 + h_brem * pow(x, 0.93) + 0.0001 * pow(x, 1.2)) *
+                          30. / (30. + 0.005 * pow(x, 2.8));
+    const double p_brem = 0.67 + 0.18 * pow(y, 0.4);
+    return pow(pow(s_nd, -p_brem) + pow(s_d, -p_brem), -1. / p_brem) * f_brem *
+           (1. + c_brem * g_brem);
+}
+
+/* kernel_brem_HR98.hpp:165-236: g-component fit, Eq.(52) */
+static double hr98_g(double y, double eta_star)
+{
+    y        = (y > C_BREM_YMIN) ? y : C_BREM_YMIN;
+    eta_star = (eta_star > C_BREM_ETAMIN) ? eta_star : C_BREM_ETAMIN;
+    const double y2    = SQ(y);
+    const double inv   = 1. / eta_star;
+    const double a1den = 25. * y2 + 1.;
+    const double a1    = (0.5 + inv) / (1. + inv) * (1. / a1den) +
+                      (0.5 + eta_star / 15.6) * 25. * y2 / a1den;
+    const double a2  = (0.63 + 0.04 * pow(eta_star, 1.45)) /
+                      (1. + 0.02 * pow(eta_star, 2.5));
+    const double p15 = pow(eta_star, 1.5);
+    const double a3  = 1.2 * safe_exp(0.6 * eta_star - 0.4 * p15);
+    const double p1  = (1.8 + 0.45 * eta_star) / (1. + 0.15 * p15);
+    const double p2  = 2.3 - 0.05 * eta_star / (1. + 0.025 * eta_star);
+    return (a1 + a2 * pow(y, p1)) /
+           (1. + a3 * pow(y, p2) + a2 * pow(y, p1 + 2.) / 13.75);
+}
+
+/* kernel_brem_HR98.hpp:239-289: one NN channel of the absorption kernel,
+ * Eq.(35) with eta*, gamma and y from Eqs.(36)-(38) */
+static double hr98_channel(double n_nuc, double m_nuc, double omega,
+                           double omega_prime, double T)
+{
+    const double x    = (omega + omega_prime) / T;
+    const double T10  = T * 0.1;
+    const double etas = pow(3. * C_PISQ * n_nuc, 2. / 3.) * C_BREM_AUX1 /
+                        (2. * m_nuc * T);
+    const double gam = 1.63 * pow(etas, 1.5) * T10;
+    const double y   = 1.94 / T10;
+    const double sb  = hr98_s(x, y, etas);
+    const double gb  = hr98_g(y, etas);
+    return gam / (SQ(x) + SQ(0.5 * gam * gb)) * sb / T;
+}
+
+/* kernel_brem_HR98.hpp:293-338 (nn + pp + 28/3 np channels, Fischer16
+ * medium correction) and :342-393 (l = 0 coefficient, detailed balance) */
+static void brem_hr98(const eos_t* eos, double omega, double omega_prime,
+                      int medium_corr, double* em, double* ab)
+{
+    const double nb    = eos->nb;
+    const double xn    = eos->yn;
+    const double xp    = eos->yp;
+    const double xmean = sqrt(xn * xp);
+    const double nn    = nb * xn;
+    const double np    = nb * xp;
+    const double nmean = nb * xmean;
+    const double snn   = hr98_channel(nn, C_MN_GRAMS, omega, omega_prime, eos->temp);
+    const double spp   = hr98_channel(np, C_MP_GRAMS, omega, omega_prime, eos->temp);
+    const double snp =
+        hr98_channel(nmean, C_MAVG_GRAMS, omega, omega_prime, eos->temp);
+    double s = C_BREM_CONST * (nn * snn + np * spp + (28. / 3.) * nmean * snp);
+    if (medium_corr)
+    {
+        const double q = (1. + cbrt(nb / C_SAT_N) / 3.);
+        s              = s / (q * q * q * q * q * q);
+    }
+    const double x = (omega + omega_prime) / eos->temp;
+    s              = 3. * s;
+    *ab            = s;
+    *em            = s * safe_exp(-x);
+}
+
+/* ===================================================================== */
+/* NN bremsstrahlung: BRT06 (kernel_brem_BRT06.hpp)                         */
+/* ===================================================================== */
+
+/* kernel_brem_BRT06.hpp:24-69 */
+static void brem_brt06(const eos_t* eos, double omega, double omega_prime,
+                       double* em, double* ab)
+{
+    const double T   = eos->temp;
+    const double x   = 0.5 * (omega + omega_prime) / T;
+    const double xn  = eos->yn, xp = eos->yp;
+    const double rho = eos->nb * C_MB;
+    const double q   = 2.0778e+02 * 0.5 * C_MEV *
+                     (SQ(xn) + SQ(xp) + (28. / 3.) * xn * xp) * SQ(rho) *
+                     pow(T, 5.5);
+    const double T7  = T * T * T * T * T * T * T;
+    const double tmp = C_HC6_4PI2 * C_BREM_C4BRT06 * (q / T7) * bessk1(x) / x;
+    *em              = tmp * safe_exp(-x);
+    *ab              = tmp * safe_exp(x);
+}
+
+/* ===================================================================== */
+/* NN bremsstrahlung: GP19 table (kernel_brem_GP19.hpp)                     */
+/* ===================================================================== */
+
+static struct
+{
+    int d[4];
+    double *nb, *ye, *t, *w, *lognb, *logw, *data;
+} gp19 = {{0, 0, 0, 0}, NULL, NULL, NULL, NULL, NULL, NULL, NULL};
+
+/* kernel_brem_GP19.hpp:35-59: first bracketing interval by linear scan */
+static int gp19_bracket(double v, const double* ax, int n, int* i0, double* t)
+{
+    if (v < ax[0] || v > ax[n - 1])
+        return -1;
+    for (int i = 0; i < n - 1; ++i)
+    {
+        if (v >= ax[i] && v <= ax[i + 1])
+        {
+            *i0 = i;
+            *t  = (v - ax[i]) / (ax[i + 1] - ax[i]);
+            return 0;
+        }
+    }
+    return -1;
+}
+
+/* kernel_brem_GP19.hpp:75-139: 4-D multilinear interpolation in
+ * (log nb, Ye, T, log w); NaN outside the table. */
+static double gp19_interp(double nb, double ye, double T, double w)
+{
+    int i, j, k, l;
+    double tx, ty, tz, tw;
+    const double lnb = log(nb), lw = log(w);
+    if (gp19_bracket(lnb, gp19.lognb, gp19.d[0], &i, &tx) < 0 ||
+        gp19_bracket(ye, gp19.ye, gp19.d[1], &j, &ty) < 0 ||
+        gp19_bracket(T, gp19.t, gp19.d[2], &k, &tz) < 0 ||
+        gp19_bracket(lw, gp19.logw, gp19.d[3], &l, &tw) < 0)
+        return NAN;
+    const int D1 = gp19.d[1], D2 = gp19.d[2], D3 = gp19.d[3];
+#define GIX(a, b, c, e) ((((a) * D1 + (b)) * D2 + (c)) * D3 + (e))
+    const double* g = gp19.data;
+    const double a0 = 1. - tx, a1 = tx, b0 = 1. - ty, b1 = ty;
+    const double c0 = 1. - tz, c1 = tz, d0 = 1. - tw, d1 = tw;
+    /* 16 hypercube vertices, summed in the reference's order */
+    const double r =
+        g[GIX(i, j, k, l)] * a0 * b0 * c0 * d0 +
+        g[GIX(i, j, k, l + 1)] * a0 * b0 * c0 * d1 +
+        g[GIX(i, j, k + 1, l)] * a0 * b0 * c1 * d0 +
+        g[GIX(i, j, k + 1, l + 1)] * a0 * b0 * c1 * d1 +
+        g[GIX(i, j + 1, k, l)] * a0 * b1 * c0 * d0 +
+        g[GIX(i, j + 1, k, l + 1)] * a0 * b1 * c0 * d1 +
+        g[GIX(i, j + 1, k + 1, l)] * a0 * b1 * c1 * d0 +
+        g[GIX(i, j + 1, k + 1, l + 1)] * a0 * b1 * c1 * d1 +
+        g[GIX(i + 1, j, k, l)] * a1 * b0 * c0 * d0 +
+        g[GIX(i + 1, j, k, l + 1)] * a1 * b0 * c0 * d1 +
+        g[GIX(i + 1, j, k + 1, l)] * a1 * b0 * c1 * d0 +
+        g[GIX(i + 1, j, k + 1, l + 1)] * a1 * b0 * c1 * d1 +
+        g[GIX(i + 1, j + 1, k, l)] * a1 * b1 * c0 * d0 +
+        g[GIX(i + 1, j + 1, k, l + 1)] * a1 * b1 * c0 * d1 +
+        g[GIX(i + 1, j + 1, k + 1, l)] * a1 * b1 * c1 * d0 +
+        g[GIX(i + 1, j + 1, k + 1, l + 1)] * a1 * b1 * c1 * d1;
+#undef GIX
+    return r;
+}
+
+/* kernel_brem_GP19.hpp:159-172 */
+static double gp19_in_range(double nb, double ye, double T, double w)
+{
+    const double S = gp19_interp(nb, ye, T, w);
+    return C_BREM_CONST * (nb * 1e+18) * S;
+}
+
+/* kernel_brem_GP19.hpp:178-192 */
+static double gp19_low_nb(double nb, double ye, double T, double w)
+{
+    const double nbmin = gp19.nb[0];
+    const double k     = gp19_in_range(nbmin, ye, T, w);
+    return k * SQ(nb / nbmin);
+}
+
+/* kernel_brem_GP19.hpp:195-216 */
+static double gp19_low_t(double nb, double ye, double T, double w)
+{
+    const double k2 = gp19_in_range(nb, ye, 2.0, w);
+    const double k4 = gp19_in_range(nb, ye, 4.0, w);
+    const double m  = log(k4 / k2) * 1.4426950408889634;
+    return k2 * pow(T * 0.5, m);
+}
+
+/* kernel_brem_GP19.hpp:219-262 */
+static double gp19_low_nb_low_t(double nb, double ye, double T, double w)
+{
+    const double eps = 1e-30;
+    double k2        = gp19_low_nb(nb, ye, 2.0, w);
+    double k4        = gp19_low_nb(nb, ye, 4.0, w);
+    if (k2 < eps)
+        k2 = eps;
+    if (k4 < eps)
+        k4 = eps;
+    const double m = log(k4 / k2) * 1.4426950408889634;
+    double k       = k2 * pow(T * 0.5, m);
+    if (k < eps)
+        k = eps;
+    return k;
+}
+
+/* kernel_brem_GP19.hpp:265-322: Lorentzian continuation above T = 50 MeV
+ * matched to the table at T = 48 and 50 MeV */
+static double gp19_high_t(double nb, double ye, double T, double w)
+{
+    const double nbnm  = nb * 1e+18;
+    const double nbnm2 = SQ(nbnm);
+    const double w2    = SQ(w);
+    const double sqrt50 = 7.0710678118654755;
+    const double R48   = gp19_in_range(nb, ye, 48.0, w);
+    const double R50   = gp19_in_range(nb, ye, 50.0, w);
+    const double K     = 4. * C_BREM_CONST * nbnm2;
+    const double A     = 1. / R50;
+    const double A2    = SQ(A);
+    const double B     = 1. / (K * sqrt50);
+    const double B2    = SQ(B);
+    const double m     = (R50 - R48) / (50.0 - 48.0);
+    const double bnum  = 8. * w2 * K * B2;
+    const double bden1 = 2. * m * A2 * sqrt50;
+    const double bden2 = A * K * B;
+    const double beta  = bnum / (bden1 + bden2);
+    const double gnum  = (A * beta) - (4. * B * w2);
+    const double gden  = B * nbnm2 * 50.0;
+    const double gamma = gnum / gden;
+    const double l1    = (w / T) * (w / T);
+    const double l2    = (nbnm2 / (4. * T)) * gamma;
+    const double inv   = 1. / (l1 + l2);
+    const double scal  = (beta * nbnm) / (T * sqrt(T));
+    const double S     = scal * inv;
+    return C_BREM_CONST * nbnm * S;
+}
+
+/* kernel_brem_GP19.hpp:325-342 */
+static double gp19_high_t_low_nb(double nb, double ye, double T, double w)
+{
+    const double nbmin = gp19.nb[0];
+    const double k     = gp19_high_t(nbmin, ye, T, w);
+    return k * ((nb / nbmin) * (nb / nbmin));
+}
+
+/* kernel_brem_GP19.hpp:357-481: clip (Ye, nb, w) to the table, interpolate or
+ * extrapolate, take 3x (l = 0), |.|, and em by detailed balance at the
+ * unclipped pair energy. */
+static void brem_gp19(const eos_t* eos, double omega, double omega_prime,
+                      double* em, double* ab)
+{
+    double ye       = eos->ye;
+    const double T  = eos->temp;
+    double w        = omega + omega_prime;
+    const double w0 = w;
+    double nb       = eos->nb * 1e-18;
+    const int D0 = gp19.d[0], D1 = gp19.d[1], D2 = gp19.d[2], D3 = gp19.d[3];
+    const double nbmax = gp19.nb[D0 - 1], nbmin = gp19.nb[0];
+    const double yemax = gp19.ye[D1 - 1];
+    const double Tmax = gp19.t[D2 - 1], Tmin = gp19.t[0];
+    const double wmax = gp19.w[D3 - 1], wmin = gp19.w[0];
+    if (ye > yemax)
+        ye = yemax;
+    if (nb > nbmax)
+        nb = nbmax;
+    if (w > wmax)
+        w = wmax;
+    else if (w < wmin)
+        w = wmin;
+    double s = 0.;
+    if (nb >= nbmin && T >= Tmin && T <= Tmax)
+        s = gp19_in_range(nb, ye, T, w);
+    if (nb < nbmin)
+    {
+        if (T < Tmin)
+            s = gp19_low_nb_low_t(nb, ye, T, w);
+        else if (T > Tmax)
+            s = gp19_high_t_low_nb(nb, ye, T, w);
+        else
+            s = gp19_low_nb(nb, ye, T, w);
+    }
+    else if (T < Tmin)
+        s = gp19_low_t(nb, ye, T, w);
+    else if (T > Tmax)
+        s = gp19_high_t(nb, ye, T, w);
+    s   = 3. * s;
+    s   = fabs(s);
+    *ab = s;
+    *em = s * safe_exp(-w0 / T);
+}
+
+/* Brem dispatch; the three implementations are species independent. */
+static void brem_kernel(const eos_t* eos, const pars_t* p, double omega,
+                        double omega_prime, double* em, double* ab)
+{
+    if (p->brem_impl == 1)
+        brem_brt06(eos, omega, omega_prime, em, ab);
+    else if (p->brem_impl == 2)
+        brem_gp19(eos, omega, omega_prime, em, ab);
+    else
+        brem_hr98(eos, omega, omega_prime, p->use_NN_medium_corr, em, ab);
+}
+
+/* ===================================================================== */
+/* Inelastic scattering on e- / e+ (kernel_nes.hpp)                        */
+/* ===================================================================== */
+
+/* kernel_nes.hpp:29-44 */
+static void fdi_for_inelastic(double w, double wp, double eta, double* dw,
+                              double* dabs)
+{
+    const double a = fabs(w - wp);
+    dw[0]   = fdi_p1(eta - wp) - fdi_p1(eta - w);
+    dw[1]   = fdi_p2(eta - wp) - fdi_p2(eta - w);
+    dw[2]   = fdi_p3(eta - wp) - fdi_p3(eta - w);
+    dw[3]   = fdi_p4(eta - wp) - fdi_p4(eta - w);
+    dw[4]   = fdi_p5(eta - wp) - fdi_p5(eta - w);
+    dabs[0] = fdi_p3(eta) - fdi_p3(eta - a);
+    dabs[1] = fdi_p4(eta) - fdi_p4(eta - a);
+    dabs[2] = fdi_p5(eta) - fdi_p5(eta - a);
+}
+
+/* kernel_nes.hpp:50-78: unexpanded out-kernel integral (Mezzacappa & Bruenn
+ * 1993 Eq.(43)) */
+static double mb_int_out(double w, double wp, double x, double y, int sign,
+                         double b1, double b2, const double* dw,
+                         const double* dabs)
+{
+    return (((b1 + b2) * (sign * dabs[2] - dw[4]) * 0.2 -
+             b1 * (w + wp) * (dw[3] + 2. * ((w + wp) * dw[2] + 3. * w * wp * dw[1])) +
+             sign * ((b1 * x - b2 * y) * dabs[1] +
+                     2. * (b1 * x * x + b2 * y * y) * dabs[0])) /
+                (w * w * wp * wp) -
+            6. * b1 * dw[0]);
+}
+
+/* kernel_nes.hpp:82-107: Taylor expansion in the smaller energy */
+static double mb_int_one(double x, double y, int sign, double b1, double b2,
+                         const double* f)
+{
+    return -sign * y *
+           (2. * (b1 + b2) * f[0] + (b1 * (y + 4. * x) + 3. * b2 * y) * f[1] +
+            (b1 * (3. * y - 4. * x) + b2 * y) * f[2] +
+            ((b1 + 6. * b2) * y * y * 0.2 + b1 * x * y + 2. * b1 * x * x) * f[3] -
+            ((6. * b1 + b2) * y * y * 0.2 - 3. * b1 * x * y + 2. * b1 * x * x) * f[4]) /
+           (x * x);
+}
+
+/* kernel_nes.hpp:111-132: Taylor expansion in both energies */
+static double mb_int_two(double w, double wp, double x, double y, double b1,
+                         double b2, const double* f)
+{
+    return y * (w - wp) *
+           ((b1 + b2) * (4. * f[2] + f[0] * (11. * y * y - 25. * x * y + 20. * x * x) / 30.) +
+            (b1 - b2) * (2. * x - y) * f[1]) /
+           (x * x);
+}
+
+/* kernel_nes.hpp:139-340: NES (lep = +1, eta = mu_e/T) and NPS (lep = -1,
+ * eta = -mu_e/T) out/in kernels for the four species.  The (b1, b2) coupling
+ * pair of each species is swapped between electrons and positrons. */
+static void nes_nps(double temp, double mu_e, double omega, double omega_prime,
+                    int positron, kern_t* k)
+{
+    const double T   = temp;
+    const double w   = omega / T;
+    const double wp  = omega_prime / T;
+    const double x   = (w > wp) ? w : wp;
+    const double y   = (w < wp) ? w : wp;
+    const double eta = positron ? -mu_e / T : mu_e / T;
+    const double ef  = neps_exp_func(wp - w);
+    const double efx = neps_exp_func(w - wp);
+    const double BP = C_NEPS_BPLUS, BM = C_NEPS_BMINUS, BZ = C_NEPS_BZERO;
+    double b1[4], b2[4];
+    if (!positron)
+    {
+        b1[0] = BP; b2[0] = BZ;
+        b1[1] = BZ; b2[1] = BP;
+        b1[2] = BM; b2[2] = BZ;
+        b1[3] = BZ; b2[3] = BM;
+    }
+    else
+    {
+        b1[0] = BZ; b2[0] = BP;
+        b1[1] = BP; b2[1] = BZ;
+        b1[2] = BZ; b2[2] = BM;
+        b1[3] = BM; b2[3] = BZ;
+    }
+    const double pre = C_NEPS_CONST * SQ(T);
+    if (y > eta * 1e-3)
+    {
+        double dw[5], dabs[3];
+        const int sign = 2 * (signbit(wp - w) != 0) - 1;
+        fdi_for_inelastic(w, wp, eta, dw, dabs);
+        for (int s = 0; s < NSP; ++s)
+            k->ab[s] = pre * mb_int_out(w, wp, x, y, sign, b1[s], b2[s], dw, dabs);
+    }
+    else if (x > eta * 1e-3)
+    {
+        const int sign = 2 * (signbit(wp - w) != 0) - 1;
+        const double f[5] = {fdi_p2(eta - x) - fdi_p2(eta), fdi_p1(eta - x),
+                             fdi_p1(eta),
+                             fdi_0(eta - x) + y * fermi_distr(0., 1., eta - x) / 6.,
+                             fdi_0(eta) - y * fermi_distr(0., 1., eta) / 6.};
+        for (int s = 0; s < NSP; ++s)
+            k->ab[s] = pre * mb_int_one(x, y, sign, b1[s], b2[s], f);
+    }
+    else
+    {
+        const double f[3] = {fermi_distr(0., 1., eta), fdi_0(eta), fdi_p1(eta)};
+        for (int s = 0; s < NSP; ++s)
+            k->ab[s] = pre * mb_int_two(w, wp, x, y, b1[s], b2[s], f);
+    }
+    for (int s = 0; s < NSP; ++s)
+    {
+        k->em[s] = k->ab[s];
+        k->ab[s] = k->ab[s] * ef;
+        k->em[s] = -k->em[s] * efx;
+    }
+}
+
+/* kernel_nes.hpp:343-359 */
+static void inelastic_kernels(double temp, double mu_e, double omega,
+                              double omega_prime, kern_t* k)
+{
+    kern_t e, p;
+    nes_nps(temp, mu_e, omega, omega_prime, 0, &e);
+    nes_nps(temp, mu_e, omega, omega_prime, 1, &p);
+    for (int s = 0; s < NSP; ++s)
+    {
+        k->em[s] = e.em[s] + p.em[s];
+        k->ab[s] = e.ab[s] + p.ab[s];
+    }
+}
+
+/* ===================================================================== */
+/* Grey M1 opacities (m1_opacities.hpp) and quadrature (integration.hpp)   */
+/* ===================================================================== */
+
+typedef struct
+{
+    double em[NSP][MMAX][MMAX];
+    double ab[NSP][MMAX][MMAX];
+} mat2d_t;
+
+typedef struct
+{
+    eos_t eos;
+    distr_t distr;
+    double n[NSP], J[NSP];
+    flags_t flags;
+    pars_t pars;
+} point_t;
+
+/* integration.hpp:28-87: Gauss-Legendre nodes/weights on [0, 1] by Newton
+ * iteration on P_n (tolerance 1e-10) */
+static void gauss_legendre(int n, double* pts, double* wts)
+{
+    const double eps = 1.0e-10, x1 = 0., x2 = 1.;
+    const int m      = (n + 1) / 2;
+    const double xm = 0.5 * (x2 + x1), xl = 0.5 * (x2 - x1);
+    for (int i = 0; i < m; ++i)
+    {
+        double z = cos(C_PI * (i + 0.75) / (n + 0.5)), z1, pp, p1, p2, p3;
+        do
+        {
+            p1 = 1.0;
+            p2 = 0.0;
+            for (int j = 0; j < n; ++j)
+            {
+                p3 = p2;
+                p2 = p1;
+                p1 = ((2.0 * j + 1.0) * z * p2 - j * p3) / (j + 1);
+            }
+            pp = n * (z * p1 - p2) / (SQ(z) - 1.0);
+            z1 = z;
+            z  = z1 - p1 / pp;
+        } while (fabs(z - z1) > eps);
+        pts[i]         = xm - xl * z;
+        pts[n - 1 - i] = xm + xl * z;
+        wts[i]         = 2.0 * xl / ((1.0 - SQ(z)) * SQ(pp));
+        wts[n - 1 - i] = wts[i];
+    }
+}
+
+/* m1_opacities.hpp:39-91 (integrand) + integration.hpp:770-802 (sum):
+ * iso-energetic scattering J-weighted integral per species */
+static void iso_integrals(const quad_t* q, const point_t* P, const double* t,
+                          double* res)
+{
+    const int n = q->n;
+    double out[NSP][MMAX];
+    for (int i = 0; i < n; ++i)
+    {
+        for (int s = 0; s < NSP; ++s)
+        {
+            double nu   = t[s] * q->x[i];
+            double g    = total_nu_f(nu, &P->distr, s);
+            double iso  = iso_scatt_total(nu, &P->pars, &P->eos);
+            double aux  = 4 * C_PI * SQ(nu) * SQ(nu) * nu * iso;
+            out[s][i]   = g * aux;
+            nu          = t[s] / q->x[i];
+            g           = total_nu_f(nu, &P->distr, s);
+            iso         = iso_scatt_total(nu, &P->pars, &P->eos);
+            aux         = 4 * C_PI * SQ(nu) * SQ(nu) * nu * iso;
+            out[s][n + i] = g * aux;
+        }
+    }
+    for (int s = 0; s < NSP; ++s)
+    {
+        res[s] = 0.;
+        for (int i = 0; i < n; ++i)
+        {
+            const double x = q->x[i], w = q->w[i], x2 = x * x;
+            res[s] += w * (out[s][i] + out[s][n + i] / x2);
+        }
+    }
+    for (int s = 0; s < NSP; ++s)
+        res[s] *= t[s];
+}
+
+/* m1_opacities.hpp:93-237 (integrand) + integration.hpp:805-844 (number and
+ * energy weighted sums) for the beta processes of nue and anue. */
+static void beta_integrals(const quad_t* q, const point_t* P, const double* t,
+                           int stim, double* n_em, double* j_em, double* n_ab,
+                           double* j_ab)
+{
+    const int n = q->n;
+    double em[2][MMAX], ab[2][MMAX];
+    for (int i = 0; i < n; ++i)
+    {
+        for (int half = 0; half < 2; ++half)
+        {
+            for (int s = 0; s < 2; ++s)
+            {
+                const double nu  = half == 0 ? t[s] * q->x[i] : t[s] / q->x[i];
+                const double nu2 = SQ(nu);
+                const double g   = total_nu_f(nu, &P->distr, s);
+                double o[4];
+                abs_opacity(nu, &P->pars, &P->eos, stim, o);
+                const double e  = s == 0 ? o[1] : o[3];
+                const double a  = s == 0 ? o[0] : o[2];
+                em[s][half * n + i] = nu2 * e;
+                ab[s][half * n + i] = nu2 * g * a;
+            }
+        }
+    }
+    for (int pass = 0; pass < 2; ++pass)
+    {
+        double(*mat)[MMAX] = pass == 0 ? em : ab;
+        double* on         = pass == 0 ? n_em : n_ab;
+        double* oj         = pass == 0 ? j_em : j_ab;
+        for (int s = 0; s < 2; ++s)
+        {
+            on[s] = 0.;
+            oj[s] = 0.;
+            for (int i = 0; i < n; ++i)
+            {
+                const double x = q->x[i], w = q->w[i], x2 = SQ(x);
+                on[s] += w * (mat[s][i] + mat[s][n + i] / x2);
+                oj[s] += w * (mat[s][i] * t[s] * x + mat[s][n + i] * (t[s] / x) / x2);
+            }
+            on[s] *= t[s];
+            oj[s] *= t[s];
+        }
+    }
+}
+
+static double blocking(const point_t* P, double g)
+{
+    return P->pars.neglect_blocking ? 1. : 1. - g;
+}
+
+/* partner species whose occupation blocks/enables the pair reactions */
+static const int partner[NSP] = {ANUE, NUE, ANUX, NUX};
+
+/* m1_opacities.hpp:774-862 with :289-340 (pair), :343-478 (brem),
+ * :577-660 (distribution weights) and :662-758 (nu^2 nubar^2 weights and
+ * stimulated absorption) */
+static void double_integrand(const quad_t* q, double t, const point_t* P,
+                             int stim, mat2d_t* out)
+{
+    const int n = q->n, M = 2 * n;
+    double nu[MMAX];
+    memset(out, 0, sizeof(*out));
+    for (int i = 0; i < n; ++i)
+    {
+        nu[i]     = t * q->x[i];
+        nu[n + i] = t / q->x[i];
+    }
+    if (P->flags.use_pair)
+    {
+        for (int i = 0; i < M; ++i)
+        {
+            kern_t k;
+            pair_kernels(P->eos.temp, P->eos.mu_e, nu[i], nu[i], &k);
+            for (int s = 0; s < NSP; ++s)
+            {
+                out->em[s][i][i] += k.em[s];
+                out->ab[s][i][i] += k.ab[s];
+            }
+            for (int j = i + 1; j < M; ++j)
+            {
+                pair_kernels(P->eos.temp, P->eos.mu_e, nu[i], nu[j], &k);
+                for (int s = 0; s < NSP; ++s)
+                {
+                    out->em[s][i][j] += k.em[s];
+                    out->em[s][j][i] += k.em[partner[s]];
+                    out->ab[s][i][j] += k.ab[s];
+                    out->ab[s][j][i] += k.ab[partner[s]];
+                }
+            }
+        }
+    }
+    if (P->flags.use_brem)
+    {
+        for (int i = 0; i < M; ++i)
+        {
+            for (int j = i; j < M; ++j)
+            {
+                double em, ab;
+                brem_kernel(&P->eos, &P->pars, nu[i], nu[j], &em, &ab);
+                for (int s = 0; s < NSP; ++s)
+                {
+                    out->em[s][i][j] += em;
+                    out->ab[s][i][j] += ab;
+                    if (j != i)
+                    {
+                        out->em[s][j][i] += em;
+                        out->ab[s][j][i] += ab;
+                    }
+                }
+            }
+        }
+    }
+    if (P->flags.use_pair || P->flags.use_brem)
+    {
+        for (int i = 0; i < M; ++i)
+        {
+            double g[NSP], bf[NSP];
+            for (int s = 0; s < NSP; ++s)
+            {
+                g[s]  = total_nu_f(nu[i], &P->distr, s);
+                bf[s] = blocking(P, g[s]);
+            }
+            for (int s = 0; s < NSP; ++s)
+            {
+                out->em[s][i][i] *= bf[partner[s]];
+                out->ab[s][i][i] *= g[partner[s]];
+            }
+            for (int j = i + 1; j < M; ++j)
+            {
+                double gb[NSP], bfb[NSP];
+                for (int s = 0; s < NSP; ++s)
+                {
+                    gb[s]  = total_nu_f(nu[j], &P->distr, s);
+                    bfb[s] = blocking(P, gb[s]);
+                }
+                for (int s = 0; s < NSP; ++s)
+                {
+                    out->em[s][i][j] *= bfb[partner[s]];
+                    out->em[s][j][i] *= bf[partner[s]];
+                    out->ab[s][i][j] *= gb[partner[s]];
+                    out->ab[s][j][i] *= g[partner[s]];
+                }
+            }
+        }
+    }
+    for (int i = 0; i < M; ++i)
+    {
+        const double nu2 = SQ(nu[i]);
+        double g[NSP];
+        double w4 = SQ(nu2);
+        for (int s = 0; s < NSP; ++s)
+        {
+            g[s] = total_nu_f(nu[i], &P->distr, s);
+            if (stim)
+            {
+                out->ab[s][i][i] = w4 * g[s] * (out->em[s][i][i] + out->ab[s][i][i]);
+                out->em[s][i][i] *= w4;
+            }
+            else
+            {
+                out->ab[s][i][i] *= w4 * g[s];
+                out->em[s][i][i] *= w4 * (1. - g[s]);
+            }
+        }
+        for (int j = i + 1; j < M; ++j)
+        {
+            w4 = nu2 * SQ(nu[j]);
+            for (int s = 0; s < NSP; ++s)
+            {
+                const double gb = total_nu_f(nu[j], &P->distr, s);
+                if (stim)
+                {
+                    out->ab[s][i][j] = w4 * g[s] * (out->em[s][i][j] + out->ab[s][i][j]);
+                    out->ab[s][j][i] = w4 * gb * (out->em[s][j][i] + out->ab[s][j][i]);
+                    out->em[s][i][j] *= w4;
+                    out->em[s][j][i] *= w4;
+                }
+                else
+                {
+                    out->ab[s][i][j] *= w4 * g[s];
+                    out->ab[s][j][i] *= w4 * gb;
+                    out->em[s][i][j] *= w4 * (1. - g[s]);
+                    out->em[s][j][i] *= w4 * (1. - gb);
+                }
+            }
+        }
+    }
+}
+
+/* integration.hpp:608-685: number (r1) and energy (r2) moments of the 2-D
+ * matrix over the four quadrants [0,t]x[0,t] ... [t,inf)x[t,inf) */
+static void integrate_2d_m1(const quad_t* q, const mat2d_t* m, double t,
+                            double* r1, double* r2)
+{
+    const int n = q->n;
+    const double t2 = t * t;
+    for (int k = 0; k < 2 * NSP; ++k)
+        r1[k] = r2[k] = 0.;
+    for (int s = 0; s < NSP; ++s)
+    {
+        for (int i = 0; i < n; ++i)
+        {
+            const double xi = q->x[i], wi = q->w[i], x2i = xi * xi;
+            const double a1 = t * xi, a2 = t / (xi * x2i);
+            for (int j = 0; j < n; ++j)
+            {
+                const double xj = q->x[j], wj = q->w[j];
+                const double wij = wi * wj, x2j = xj * xj, x2ij = x2i * x2j;
+                const double a3 = a1 / x2j, a4 = a2 / x2j;
+                r1[s] += wij * (m->em[s][i][j] + m->em[s][n + i][j] / x2i +
+                                m->em[s][i][n + j] / x2j +
+                                m->em[s][n + i][n + j] / x2ij);
+                r1[NSP + s] += wij * (m->ab[s][i][j] + m->ab[s][n + i][j] / x2i +
+                                      m->ab[s][i][n + j] / x2j +
+                                      m->ab[s][n + i][n + j] / x2ij);
+                r2[s] += wij * (m->em[s][i][j] * a1 + m->em[s][n + i][j] * a2 +
+                                m->em[s][i][n + j] * a3 +
+                                m->em[s][n + i][n + j] * a4);
+                r2[NSP + s] += wij * (m->ab[s][i][j] * a1 + m->ab[s][n + i][j] * a2 +
+                                      m->ab[s][i][n + j] * a3 +
+                                      m->ab[s][n + i][n + j] * a4);
+            }
+        }
+    }
+    for (int k = 0; k < 2 * NSP; ++k)
+    {
+        r1[k] *= t2;
+        r2[k] *= t2;
+    }
+}
+
+/* m1_opacities.hpp:864-1057: NES/NPS 2-D integrand on the (x_i, x_j) grid,
+ * nu = t x_i (1 -+ x_j)/2 and t (1 -+ x_j)/(2 x_i) */
+static void neps_integrand(const quad_t* q, double t, const point_t* P,
+                           int stim, mat2d_t* out)
+{
+    const int n = q->n;
+    memset(out, 0, sizeof(*out));
+    for (int i = 0; i < n; ++i)
+    {
+        const double xi = q->x[i];
+        for (int j = 0; j < n; ++j)
+        {
+            const double xj = q->x[j];
+            for (int region = 0; region < 2; ++region)
+            {
+                double nu, nub;
+                if (region == 0)
+                {
+                    nu  = 0.5 * t * xi * (1. - xj);
+                    nub = 0.5 * t * xi * (1. + xj);
+                }
+                else
+                {
+                    nu  = 0.5 * t * (1. - xj) / xi;
+                    nub = 0.5 * t * (1. + xj) / xi;
+                }
+                const double w4 = SQ(nu) * SQ(nub);
+                double g[NSP], gb[NSP], bf[NSP], bfb[NSP];
+                for (int s = 0; s < NSP; ++s)
+                {
+                    g[s]   = total_nu_f(nu, &P->distr, s);
+                    gb[s]  = total_nu_f(nub, &P->distr, s);
+                    bf[s]  = blocking(P, g[s]);
+                    bfb[s] = blocking(P, gb[s]);
+                }
+                kern_t k1, k2;
+                inelastic_kernels(P->eos.temp, P->eos.mu_e, nu, nub, &k1);
+                inelastic_kernels(P->eos.temp, P->eos.mu_e, nub, nu, &k2);
+                const int r = region * n + i;
+                for (int s = 0; s < NSP; ++s)
+                {
+                    const double e1 = k1.em[s] * gb[s];
+                    const double a1 = k1.ab[s] * bfb[s];
+                    const double e2 = k2.em[s] * g[s];
+                    const double a2 = k2.ab[s] * bf[s];
+                    if (stim)
+                    {
+                        out->ab[s][r][j]     = w4 * g[s] * (e1 + a1);
+                        out->em[s][r][j]     = w4 * e1;
+                        out->ab[s][r][n + j] = w4 * gb[s] * (e2 + a2);
+                        out->em[s][r][n + j] = w4 * e2;
+                    }
+                    else
+                    {
+                        out->ab[s][r][j]     = w4 * g[s] * a1;
+                        out->em[s][r][j]     = w4 * (1. - g[s]) * e1;
+                        out->ab[s][r][n + j] = w4 * gb[s] * a2;
+                        out->em[s][r][n + j] = w4 * (1. - gb[s]) * e2;
+                    }
+                }
+            }
+        }
+    }
+}
+
+/* integration.hpp:687-768 */
+static void integrate_2d_neps(const quad_t* q, const mat2d_t* m, double t,
+                              double* r1, double* r2)
+{
+    const int n = q->n;
+    const double t2 = SQ(t);
+    for (int k = 0; k < 2 * NSP; ++k)
+        r1[k] = r2[k] = 0.;
+    for (int s = 0; s < NSP; ++s)
+    {
+        for (int i = 0; i < n; ++i)
+        {
+            const double xi = q->x[i], wi = q->w[i], x3i = xi * xi * xi;
+            for (int j = 0; j < n; ++j)
+            {
+                const double xj = q->x[j], wj = q->w[j], wij = wi * wj;
+                const double b1 = 0.5 * t * xi * (1. - xj);
+                const double b2 = 0.5 * t * xi * (1. + xj);
+                const double b3 = 0.5 * t * (1. - xj) / xi;
+                const double b4 = 0.5 * t * (1. + xj) / xi;
+                r1[s] += wij * (xi * (m->em[s][i][j] + m->em[s][i][n + j]) +
+                                (m->em[s][n + i][j] + m->em[s][n + i][n + j]) / x3i);
+                r1[NSP + s] += wij * (xi * (m->ab[s][i][j] + m->ab[s][i][n + j]) +
+                                      (m->ab[s][n + i][j] + m->ab[s][n + i][n + j]) / x3i);
+                r2[s] += wij * (xi * (b1 * m->em[s][i][j] + b2 * m->em[s][i][n + j]) +
+                                (b3 * m->em[s][n + i][j] + b4 * m->em[s][n + i][n + j]) /
+                                    x3i);
+                r2[NSP + s] +=
+                    wij * (xi * (b1 * m->ab[s][i][j] + b2 * m->ab[s][i][n + j]) +
+                           (b3 * m->ab[s][n + i][j] + b4 * m->ab[s][n + i][n + j]) / x3i);
+            }
+        }
+    }
+    for (int k = 0; k < 2 * NSP; ++k)
+    {
+        r1[k] *= 0.5 * t2;
+        r2[k] *= 0.5 * t2;
+    }
+}
+
+/* m1_opacities.hpp:1062-1295: grey M1 emissivities and opacities.
+ * out[20] = eta_0[4], kappa_0_a[4], eta[4], kappa_a[4], kappa_s[4] */
+static void m1_opacities(const quad_t* q1, const quad_t* q2, const point_t* P,
+                         int stim, double* out)
+{
+    const double* n = P->n;
+    const double* J = P->J;
+    const double temp  = P->eos.temp;
+    const double eta_e = P->eos.mu_e / temp;
+    const double s_pair = (0.5 * 4.364) * temp;
+    const double s_nux  = 1.5 * temp;
+    const double s_neps = (0.5 * 4.364) * temp;
+    double s_beta[NSP] = {0., 0., 0., 0.}, s_iso[NSP];
+
+    if (eta_e > -30. && eta_e < 30.)
+    {
+        s_beta[NUE]  = temp * fdi_p5(eta_e) / fdi_p4(eta_e);
+        s_beta[ANUE] = temp * fdi_p5(-eta_e) / fdi_p4(-eta_e);
+    }
+    else if (eta_e > 30.)
+    {
+        s_beta[NUE]  = temp * eta_e * 0.8333333333333333;
+        s_beta[ANUE] = temp * 5.;
+    }
+    else
+    {
+        s_beta[NUE]  = temp * 5.;
+        s_beta[ANUE] = temp * eta_e * 0.8333333333333333;
+    }
+    for (int s = 0; s < NSP; ++s)
+        s_iso[s] = (n[s] > 1e-21) ? (J[s] / n[s]) : s_nux;
+
+    double iso[NSP] = {0., 0., 0., 0.};
+    if (P->flags.use_iso)
+        iso_integrals(q1, P, s_iso, iso);
+
+    double bne[2] = {0., 0.}, bje[2] = {0., 0.}, bna[2] = {0., 0.},
+           bja[2] = {0., 0.};
+    if (P->flags.use_abs_em)
+        beta_integrals(q1, P, s_beta, stim, bne, bje, bna, bja);
+
+    double n2d[2 * NSP] = {0}, e2d[2 * NSP] = {0};
+    static __thread mat2d_t mat;
+    if (P->flags.use_pair || P->flags.use_brem)
+    {
+        double_integrand(q2, s_pair, P, stim, &mat);
+        integrate_2d_m1(q2, &mat, s_pair, n2d, e2d);
+    }
+    double nne[2 * NSP] = {0}, ene[2 * NSP] = {0};
+    if (P->flags.use_inelastic_scatt)
+    {
+        neps_integrand(q2, 4. * s_neps, P, stim, &mat);
+        integrate_2d_neps(q2, &mat, 4. * s_neps, nne, ene);
+    }
+
+    const double F  = C_FOURPI_HC3;
+    const double F2 = C_FOURPI_HC3_SQR;
+    const double c  = C_CLIGHT;
+    double* eta0 = out;
+    double* k0a  = out + 4;
+    double* eta  = out + 8;
+    double* ka   = out + 12;
+    double* ks   = out + 16;
+    for (int s = 0; s < NSP; ++s)
+        k0a[s] = ka[s] = ks[s] = 0.;
+
+    /* electron-type neutrinos and antineutrinos: 2-D + NES + beta */
+    for (int s = 0; s < 2; ++s)
+    {
+        eta0[s] = F * (F * (n2d[s] + nne[s]) + bne[s]);
+        eta[s]  = F * (F * (e2d[s] + ene[s]) + bje[s]);
+        if (n[s] > 1e-21)
+            k0a[s] = F / (c * n[s]) * (F * (n2d[4 + s] + nne[4 + s]) + bna[s]);
+        if (J[s] > 1e-25)
+        {
+            if (s == NUE)
+                ka[s] = n[s] == 0. ? 0. :
+                                      F / (c * J[s]) * (F * (e2d[4 + s] + ene[4 + s]) + bja[s]);
+            else
+                ka[s] = F / (c * J[s]) * (F * (e2d[4 + s] + ene[4 + s]) + bja[s]);
+            ks[s] = F / (c * J[s]) * iso[s];
+        }
+    }
+    /* heavy-lepton neutrinos and antineutrinos: 2-D + NES only */
+    for (int s = 2; s < 4; ++s)
+    {
+        eta0[s] = F2 * (n2d[s] + nne[s]);
+        eta[s]  = F2 * (e2d[s] + ene[s]);
+        if (n[s] > 1e-21)
+        {
+            if (s == ANUX)
+                k0a[s] = n[s] == 0. ? 0. : F2 / (c * n[s]) * (n2d[4 + s] + nne[4 + s]);
+            else
+                k0a[s] = F2 / (c * n[s]) * (n2d[4 + s] + nne[4 + s]);
+        }
+        if (J[s] > 1e-25)
+        {
+            ka[s] = F2 / (c * J[s]) * (e2d[4 + s] + ene[4 + s]);
+            ks[s] = F / (c * J[s]) * iso[s];
+        }
+    }
+}
+
+/* ===================================================================== */
+/* Spectral opacities (m1_opacities.hpp:1317-1660)                          */
+/* ===================================================================== */
+
+/* m1_opacities.hpp:1317-1501: the 8 integrands (production and
+ * annihilation, 4 species) at antineutrino energy nub for fixed nu; only
+ * the reactions in `fl` contribute. */
+static void spectral_integrand(double nu, double nub, const point_t* P,
+                               const flags_t* fl, double* res)
+{
+    double g[NSP], gb[NSP], bf[NSP];
+    for (int s = 0; s < NSP; ++s)
+    {
+        g[s]  = total_nu_f(nu, &P->distr, s);
+        gb[s] = total_nu_f(nub, &P->distr, s);
+    }
+    kern_t pk = {{0, 0, 0, 0}, {0, 0, 0, 0}}, bk = pk, ik = pk;
+    if (fl->use_pair)
+        pair_kernels(P->eos.temp, P->eos.mu_e, nu, nub, &pk);
+    if (fl->use_brem)
+    {
+        double em, ab;
+        brem_kernel(&P->eos, &P->pars, nu, nub, &em, &ab);
+        for (int s = 0; s < NSP; ++s)
+        {
+            bk.em[s] = em;
+            bk.ab[s] = ab;
+        }
+    }
+    if (fl->use_inelastic_scatt)
+        inelastic_kernels(P->eos.temp, P->eos.mu_e, nu, nub, &ik);
+    for (int s = 0; s < NSP; ++s)
+        bf[s] = P->pars.neglect_blocking ? 1. : 1. - gb[s];
+    double pro[NSP], ann[NSP];
+    for (int s = 0; s < NSP; ++s)
+    {
+        pro[s] = (pk.em[s] + bk.em[s]) * bf[partner[s]];
+        pro[s] += ik.em[s] * gb[s];
+    }
+    for (int s = 0; s < NSP; ++s)
+    {
+        ann[s] = (pk.ab[s] + bk.ab[s]) * gb[partner[s]];
+        ann[s] += ik.ab[s] * bf[s];
+    }
+    (void)g;
+    for (int s = 0; s < NSP; ++s)
+    {
+        res[s]       = SQ(nub) * pro[s];
+        res[NSP + s] = SQ(nub) * ann[s];
+    }
+}
+
+/* integration.hpp:510-546: 8 integrals, each over [0,t] U [t,inf); as in the
+ * reference the full integrand is evaluated once per (integral, node). */
+static void integrate_1d_spectral(const quad_t* q, double nu, const point_t* P,
+                                  const flags_t* fl, const double* t,
+                                  double* res)
+{
+    const int n = q->n;
+    for (int k = 0; k < 2 * NSP; ++k)
+    {
+        double f1[NMAX], f2[NMAX], v[2 * NSP];
+        for (int i = 0; i < n; ++i)
+        {
+            spectral_integrand(nu, t[k] * q->x[i], P, fl, v);
+            f1[i] = v[k];
+            spectral_integrand(nu, t[k] / q->x[i], P, fl, v);
+            f2[i] = v[k] / (q->x[i] * q->x[i]);
+        }
+        double a = 0., b = 0.;
+        for (int i = 0; i < n; ++i)
+            a += q->w[i] * f1[i];
+        for (int i = 0; i < n; ++i)
+            b += q->w[i] * f2[i];
+        res[k] = t[k] * (a + b);
+    }
+}
+
+/* m1_opacities.hpp:1506-1660: out[16] = j[4], kappa[4], j_s[4], kappa_s[4] */
+static void spectral_opacities(double nu, const quad_t* q, const point_t* P,
+                               int stim, double* out)
+{
+    const double c = C_CLIGHT;
+    double g[NSP];
+    for (int s = 0; s < NSP; ++s)
+        g[s] = total_nu_f(nu, &P->distr, s);
+    double s_pair[2 * NSP], s_neps[2 * NSP];
+    for (int k = 0; k < 2 * NSP; ++k)
+    {
+        s_pair[k] = (0.5 * 4.364) * P->eos.temp;
+        s_neps[k] = nu;
+    }
+    flags_t fl = P->flags;
+    fl.use_inelastic_scatt = 0;
+    double ip[2 * NSP], in[2 * NSP] = {0};
+    integrate_1d_spectral(q, nu, P, &fl, s_pair, ip);
+    if (P->flags.use_inelastic_scatt)
+    {
+        flags_t fn = {0, 0, 0, 1, 0};
+        integrate_1d_spectral(q, nu, P, &fn, s_neps, in);
+    }
+    double beta[4] = {0., 0., 0., 0.};
+    if (P->flags.use_abs_em)
+        abs_opacity(nu, &P->pars, &P->eos, 0, beta);
+    double iso = 0.;
+    if (P->flags.use_iso)
+        iso = iso_scatt_leg_coeff(nu, &P->pars, &P->eos, 0);
+    const double b_em[4] = {beta[1], beta[3], 0., 0.};
+    const double b_ab[4] = {beta[0], beta[2], 0., 0.};
+    double* j   = out;
+    double* kap = out + 4;
+    double* js  = out + 8;
+    double* ks  = out + 12;
+    for (int s = 0; s < NSP; ++s)
+    {
+        j[s]   = b_em[s] + C_FOURPI_HC3 * (ip[s] + in[s]);
+        kap[s] = (b_ab[s] + C_FOURPI_HC3 * (ip[4 + s] + in[4 + s])) / c;
+        js[s]  = 4 * C_PI * SQ(nu) * g[s] * iso;
+        ks[s]  = 4 * C_PI * SQ(nu) * (1. - g[s]) * iso / c;
+    }
+    if (stim)
+    {
+        for (int s = 0; s < NSP; ++s)
+        {
+            kap[s] = j[s] / c + kap[s];
+            ks[s]  = js[s] / c + ks[s];
+        }
+    }
+}
+
+/* ===================================================================== */
+/* Batch drivers (the role of the Kokkos RangePolicy of tests/tests.hpp)   */
+/* ===================================================================== */
+
+static void load_point(point_t* P, const double* eos, const double* m1,
+                       const double* distr, const int* flags, const int* pars,
+                       int64_t np, int64_t p)
+{
+    P->eos.nb     = eos[0 * np + p];
+    P->eos.temp   = eos[1 * np + p];
+    P->eos.ye     = eos[2 * np + p];
+    P->eos.yp     = eos[3 * np + p];
+    P->eos.yn     = eos[4 * np + p];
+    P->eos.mu_p   = eos[5 * np + p];
+    P->eos.mu_n   = eos[6 * np + p];
+    P->eos.mu_e   = eos[7 * np + p];
+    P->eos.mu_mu  = eos[8 * np + p];
+    P->eos.dU     = eos[9 * np + p];
+    P->eos.dm_eff = eos[10 * np + p];
+    double chi[NSP];
+    for (int s = 0; s < NSP; ++s)
+    {
+        P->n[s] = m1[(0 + s) * np + p];
+        P->J[s] = m1[(4 + s) * np + p];
+        chi[s]  = m1[(8 + s) * np + p];
+    }
+    P->flags.use_abs_em          = flags[0];
+    P->flags.use_pair            = flags[1];
+    P->flags.use_brem            = flags[2];
+    P->flags.use_inelastic_scatt = flags[3];
+    P->flags.use_iso             = flags[4];
+    P->pars.use_dU               = pars[0] != 0;
+    P->pars.use_dm_eff           = pars[1] != 0;
+    P->pars.use_WM_ab            = pars[2] != 0;
+    P->pars.use_WM_sc            = pars[3] != 0;
+    P->pars.use_decay            = pars[4] != 0;
+    P->pars.brem_impl            = pars[5];
+    P->pars.use_NN_medium_corr   = pars[6] != 0;
+    P->pars.neglect_blocking     = pars[7] != 0;
+    if (distr)
+    {
+        for (int s = 0; s < NSP; ++s)
+        {
+            P->distr.w_t[s]    = distr[(0 + s) * np + p];
+            P->distr.temp_t[s] = distr[(4 + s) * np + p];
+            P->distr.eta_t[s]  = distr[(8 + s) * np + p];
+            P->distr.w_f[s]    = distr[(12 + s) * np + p];
+            P->distr.temp_f[s] = distr[(16 + s) * np + p];
+            P->distr.c_f[s]    = distr[(20 + s) * np + p];
+            P->distr.beta_f[s] = distr[(24 + s) * np + p];
+        }
+    }
+    else
+    {
+        distr_from_m1(P->n, P->J, chi, &P->distr);
+    }
+}
+
+static void make_quad(quad_t* q, int n, const double* x, const double* w)
+{
+    q->n = n;
+    for (int i = 0; i < n; ++i)
+    {
+        q->x[i] = x[i];
+        q->w[i] = w[i];
+    }
+}
+
+int oracle_n_max(void) { return NMAX; }
+
+void oracle_gauss_legendre(int n, double* x, double* w) { gauss_legendre(n, x, w); }
+
+int oracle_gp19_set_table(const int* dims, const double* nb, const double* ye,
+                          const double* t, const double* w, const double* lognb,
+                          const double* logw, const double* data)
+{
+    const double* src[7] = {nb, ye, t, w, lognb, logw, data};
+    double** dst[7] = {&gp19.nb, &gp19.ye, &gp19.t, &gp19.w,
+                       &gp19.lognb, &gp19.logw, &gp19.data};
+    const int64_t len[7] = {dims[0], dims[1], dims[2], dims[3], dims[0], dims[3],
+                            (int64_t)dims[0] * dims[1] * dims[2] * dims[3]};
+    for (int k = 0; k < 7; ++k)
+    {
+        free(*dst[k]);
+        *dst[k] = (double*)malloc(sizeof(double) * (size_t)len[k]);
+        if (!*dst[k])
+            return 1;
+        memcpy(*dst[k], src[k], sizeof(double) * (size_t)len[k]);
+    }
+    for (int k = 0; k < 4; ++k)
+        gp19.d[k] = dims[k];
+    return 0;
+}
+
+static int check_gp19(const int* pars, const int* flags)
+{
+    return flags[2] && pars[5] == 2 && gp19.data == NULL;
+}
+
+int oracle_m1_opacities_batch(int64_t npts, const double* eos, const double* m1,
+                              const double* distr, const int* flags,
+                              const int* pars, int nx1, const double* x1,
+                              const double* w1, int nx2, const double* x2,
+                              const double* w2, int stim_abs, double* out,
+                              int nthreads)
+{
+    if (nx1 < 1 || nx2 < 1 || nx1 > NMAX || nx2 > NMAX)
+        return 2;
+    if (check_gp19(pars, flags))
+        return 5;
+    quad_t q1, q2;
+    make_quad(&q1, nx1, x1, w1);
+    make_quad(&q2, nx2, x2, w2);
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+    for (int64_t p = 0; p < npts; ++p)
+    {
+        point_t P;
+        double o[20];
+        load_point(&P, eos, m1, distr, flags, pars, npts, p);
+        m1_opacities(&q1, &q2, &P, stim_abs, o);
+        for (int k = 0; k < 20; ++k)
+            out[k * npts + p] = o[k];
+    }
+    return 0;
+}
+
+int oracle_spectral_batch(int64_t npts, const double* eos, const double* m1,
+                          const double* distr, const int* flags, const int* pars,
+                          int nx, const double* x, const double* w, int ne,
+                          const double* energies, int stimulated, double* out,
+                          int nthreads)
+{
+    if (nx < 1 || nx > NMAX)
+        return 2;
+    if (check_gp19(pars, flags))
+        return 5;
+    quad_t q;
+    make_quad(&q, nx, x, w);
+    const int64_t tot = npts * (int64_t)ne;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads)
+    for (int64_t p = 0; p < npts; ++p)
+    {
+        point_t P;
+        load_point(&P, eos, m1, distr, flags, pars, npts, p);
+        for (int e = 0; e < ne; ++e)
+        {
+            double o[16];
+            spectral_opacities(energies[e], &q, &P, stimulated, o);
+            for (int k = 0; k < 16; ++k)
+                out[k * tot + p * ne + e] = o[k];
+        }
+    }
+    return 0;
+}
+
+void oracle_distr_from_m1_batch(int64_t npts, const double* eos,
+                                const double* m1, double* distr)
+{
+    (void)eos;
+    for (int64_t p = 0; p < npts; ++p)
+    {
+        double n[NSP], J[NSP], chi[NSP];
+        distr_t d;
+        for (int s = 0; s < NSP; ++s)
+        {
+            n[s]   = m1[(0 + s) * npts + p];
+            J[s]   = m1[(4 + s) * npts + p];
+            chi[s] = m1[(8 + s) * npts + p];
+        }
+        distr_from_m1(n, J, chi, &d);
+        for (int s = 0; s < NSP; ++s)
+        {
+            distr[(0 + s) * npts + p]  = d.w_t[s];
+            distr[(4 + s) * npts + p]  = d.temp_t[s];
+            distr[(8 + s) * npts + p]  = d.eta_t[s];
+            distr[(12 + s) * npts + p] = d.w_f[s];
+            distr[(16 + s) * npts + p] = d.temp_f[s];
+            distr[(20 + s) * npts + p] = d.c_f[s];
+            distr[(24 + s) * npts + p] = d.beta_f[s];
+        }
+    }
+}
+
+/* distribution.hpp:253-290 and :447-473 */
+void oracle_nu_equilibrium_batch(int64_t npts, const double* eos, double* distr,
+                                 double* m1)
+{
+    for (int64_t p = 0; p < npts; ++p)
+    {
+        eos_t e;
+        e.temp = eos[1 * npts + p];
+        e.mu_p = eos[5 * npts + p];
+        e.mu_n = eos[6 * npts + p];
+        e.mu_e = eos[7 * npts + p];
+        distr_t d;
+        nu_equilibrium(&e, &d);
+        const double npre = C_FOURPI_HC3 * CUBE(e.temp);
+        const double jpre = npre * e.temp;
+        for (int s = 0; s < NSP; ++s)
+        {
+            distr[(0 + s) * npts + p]  = d.w_t[s];
+            distr[(4 + s) * npts + p]  = d.temp_t[s];
+            distr[(8 + s) * npts + p]  = d.eta_t[s];
+            distr[(12 + s) * npts + p] = d.w_f[s];
+            distr[(16 + s) * npts + p] = d.temp_f[s];
+            distr[(20 + s) * npts + p] = d.c_f[s];
+            distr[(24 + s) * npts + p] = d.beta_f[s];
+            m1[(0 + s) * npts + p]     = npre * fdi_p2(d.eta_t[s]);
+            m1[(4 + s) * npts + p]     = jpre * fdi_p3(d.eta_t[s]);
+            m1[(8 + s) * npts + p]     = 1. / 3.;
+        }
+    }
+}
+
+/* ---- unit-level entry points (same shapes as oracle/ref_driver.cpp) ---- */
+
+void oracle_fdi(int k, int64_t n, const double* x, double* out)
+{
+    for (int64_t i = 0; i < n; ++i)
+    {
+        switch (k)
+        {
+        case 0: out[i] = fdi_0(x[i]); break;
+        case 1: out[i] = fdi_p1(x[i]); break;
+        case 2: out[i] = fdi_p2(x[i]); break;
+        case 3: out[i] = fdi_p3(x[i]); break;
+        case 4: out[i] = fdi_p4(x[i]); break;
+        default: out[i] = fdi_p5(x[i]); break;
+        }
+    }
+}
+
+void oracle_pair_kernel(double temp, double mu_e, double omega,
+                        double omega_prime, double* out)
+{
+    kern_t k;
+    pair_kernels(temp, mu_e, omega, omega_prime, &k);
+    for (int s = 0; s < NSP; ++s)
+    {
+        out[s]     = k.em[s];
+        out[4 + s] = k.ab[s];
+    }
+}
+
+static void eos_from11(eos_t* e, const double* v)
+{
+    e->nb     = v[0];
+    e->temp   = v[1];
+    e->ye     = v[2];
+    e->yp     = v[3];
+    e->yn     = v[4];
+    e->mu_p   = v[5];
+    e->mu_n   = v[6];
+    e->mu_e   = v[7];
+    e->mu_mu  = v[8];
+    e->dU     = v[9];
+    e->dm_eff = v[10];
+}
+
+static void pars_from8(pars_t* p, const int* v)
+{
+    p->use_dU             = v[0] != 0;
+    p->use_dm_eff         = v[1] != 0;
+    p->use_WM_ab          = v[2] != 0;
+    p->use_WM_sc          = v[3] != 0;
+    p->use_decay          = v[4] != 0;
+    p->brem_impl          = v[5];
+    p->use_NN_medium_corr = v[6] != 0;
+    p->neglect_blocking   = v[7] != 0;
+}
+
+void oracle_brem_kernel(int impl, const double* eos11, double omega,
+                        double omega_prime, int use_medium_corr, double* out)
+{
+    eos_t e;
+    eos_from11(&e, eos11);
+    pars_t p;
+    memset(&p, 0, sizeof(p));
+    p.brem_impl          = impl;
+    p.use_NN_medium_corr = use_medium_corr;
+    brem_kernel(&e, &p, omega, omega_prime, &out[0], &out[1]);
+}
+
+void oracle_inelastic_kernel(double temp, double mu_e, double omega,
+                             double omega_prime, double* out)
+{
+    kern_t k;
+    inelastic_kernels(temp, mu_e, omega, omega_prime, &k);
+    for (int s = 0; s < NSP; ++s)
+    {
+        out[s]     = k.em[s];
+        out[4 + s] = k.ab[s];
+    }
+}
+
+void oracle_abs_opacity(const double* eos11, const int* pars, double omega,
+                        int stimulated, double* out)
+{
+    eos_t e;
+    pars_t p;
+    eos_from11(&e, eos11);
+    pars_from8(&p, pars);
+    abs_opacity(omega, &p, &e, stimulated, out);
+}
+
+void oracle_iso_scatt(const double* eos11, const int* pars, double omega, int l,
+                      double* out)
+{
+    eos_t e;
+    pars_t p;
+    eos_from11(&e, eos11);
+    pars_from8(&p, pars);
+    out[0] = iso_scatt_total(omega, &p, &e);
+    out[1] = iso_scatt_leg_coeff(omega, &p, &e, l);
+}
+
+void oracle_weak_magnetism(double omega, double* out)
+{
+    wm_abs_em(omega, &out[0], &out[1]);
+    wm_scatt(omega, 1, &out[2], &out[3]);
+    wm_scatt(omega, 2, &out[4], &out[5]);
+}
+
+void oracle_total_nu_f(const double* distr28, int64_t n, const double* omega,
+                       double* out)
+{
+    distr_t d;
+    for (int s = 0; s < NSP; ++s)
+    {
+        d.w_t[s]    = distr28[0 + s];
+        d.temp_t[s] = distr28[4 + s];
+        d.eta_t[s]  = distr28[8 + s];
+        d.w_f[s]    = distr28[12 + s];
+        d.temp_f[s] = distr28[16 + s];
+        d.c_f[s]    = distr28[20 + s];
+        d.beta_f[s] = distr28[24 + s];
+    }
+    for (int s = 0; s < NSP; ++s)
+        for (int64_t i = 0; i < n; ++i)
+            out[s * n + i] = total_nu_f(omega[i], &d, s);
+}
+
+void oracle_special(int which, int64_t n, const double* a, const double* b,
+                    const double* c, double* out)
+{
+    for (int64_t i = 0; i < n; ++i)
+    {
+        switch (which)
+        {
+        case 0: out[i] = safe_exp(a[i]); break;
+        case 1: out[i] = fermi_distr(a[i], b[i], c[i]); break;
+        case 2: out[i] = neps_exp_func(a[i]); break;
+        case 3: out[i] = bessk1(a[i]); break;
+        default: out[i] = gamma_stirling(a[i]); break;
+        }
+    }
+}
