@@ -1,0 +1,22 @@
+"""GB300-native grey and spectral neutrino opacities (bns_nurates hot path).
+
+The computation lives in the CUDA library ``libbnsn_gb300.so`` built from
+``csrc/`` for sm_103a (``python -m bns_nurates_gb300.build``).  This package
+is the Python host mirror of its C ABI (``include/bns_nurates_gb300.h``).
+"""
+
+from ._capi import (BREM_BRT06, BREM_GP19, BREM_HR98, FP64, MIXED,  # noqa: F401
+                    GreyOpacityParams, M1Opacities, MyEOSParams, MyQuadrature,
+                    NuDistributionParams, OpacityFlags, OpacityParams, SpectralOpacities)
+from .api import (BnsnError, ComputeM1Opacities, ComputeM1OpacitiesNotStimulated,  # noqa: F401
+                  ComputeSpectralOpacitiesNotStimulatedAbs,
+                  ComputeSpectralOpacitiesStimulatedAbs, distr_from_m1, flags_tuple,
+                  fp64_peak_tflops, gauss_legendre, m1_opacities, m1_opacities_host, nu_equilibrium,
+                  opacity_flags, opacity_params, params_tuple, quad_arrays, set_gp19_table,
+                  spectral_opacities, synthetic_points)
+
+
+def lib():
+    """The loaded C library (raises if it has not been built)."""
+    from . import _capi
+    return _capi.load()

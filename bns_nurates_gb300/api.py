@@ -1,0 +1,281 @@
+"""Python host API over the C ABI.
+
+Batched calls take field-major structure-of-arrays tensors on the GPU:
+``eos`` [11, N] in MyEOSParams field order (nb, temp, ye, yp, yn, mu_p, mu_n,
+mu_e, mu_mu, dU, dm_eff), ``m1`` [12, N] = n[4], J[4], chi[4], optional
+``distr`` [28, N] in NuDistributionParams order.  Grey results are [20, N] in
+M1Opacities order (eta_0[4], kappa_0_a[4], eta[4], kappa_a[4], kappa_s[4]);
+spectral results [16, N, n_energies] (j, kappa, j_s, kappa_s).
+
+The per-point helpers ``ComputeM1Opacities`` / ``ComputeSpectralOpacities*``
+keep the reference's names and arguments (m1_opacities.hpp:1297-1313,
+1506-1660) and return the reference's result structs as dicts.
+
+Nothing here computes physics: every number comes from the CUDA library, and
+the module raises if that library is missing.
+"""
+
+import ctypes
+
+import numpy as np
+
+from . import _capi as C
+
+
+class BnsnError(RuntimeError):
+    """A C-ABI call returned a non-zero bnsn_status."""
+
+    def __init__(self, status):
+        lib = C.load()
+        msg = lib.bnsn_last_error().decode() or lib.bnsn_status_string(status).decode()
+        super().__init__(f"bnsn status {status}: {msg}")
+        self.status = status
+
+
+def _check(status):
+    if status != C.OK:
+        raise BnsnError(status)
+
+
+def _addr(t, k=None):
+    """Device/host address of row k of a 2-D tensor/array (or of the array)."""
+    if hasattr(t, "data_ptr"):
+        base, stride = t.data_ptr(), (t.stride(0) * t.element_size() if t.dim() > 1 else 0)
+    else:
+        base = t.ctypes.data
+        stride = t.strides[0] if t.ndim > 1 else 0
+    return base if k is None else base + k * stride
+
+
+def _stream_handle(stream):
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    return getattr(stream, "cuda_stream", stream)
+
+
+# ---------------------------------------------------------------------------
+# struct helpers
+# ---------------------------------------------------------------------------
+
+def gauss_legendre(n):
+    """MyQuadrature with n Gauss-Legendre nodes on [0, 1] (GaussLegendre)."""
+    q = C.MyQuadrature()
+    q.nx = n
+    _check(C.load().bnsn_gauss_legendre(ctypes.byref(q)))
+    return q
+
+
+def opacity_flags(use_abs_em=1, use_pair=1, use_brem=1, use_inelastic_scatt=1, use_iso=1):
+    return C.OpacityFlags(int(use_abs_em), int(use_pair), int(use_brem),
+                          int(use_inelastic_scatt), int(use_iso))
+
+
+def opacity_params(use_dU=True, use_dm_eff=False, use_WM_ab=True, use_WM_sc=True,
+                   use_decay=True, brem_implementation=C.BREM_HR98, use_NN_medium_corr=True,
+                   neglect_blocking=False):
+    return C.OpacityParams(bool(use_dU), bool(use_dm_eff), bool(use_WM_ab), bool(use_WM_sc),
+                           bool(use_decay), int(brem_implementation),
+                           bool(use_NN_medium_corr), bool(neglect_blocking))
+
+
+def flags_tuple(f):
+    return (f.use_abs_em, f.use_pair, f.use_brem, f.use_inelastic_scatt, f.use_iso)
+
+
+def params_tuple(p):
+    return (int(p.use_dU), int(p.use_dm_eff), int(p.use_WM_ab), int(p.use_WM_sc),
+            int(p.use_decay), int(p.brem_implementation), int(p.use_NN_medium_corr),
+            int(p.neglect_blocking))
+
+
+def quad_arrays(q):
+    n = q.nx
+    return np.array(q.points[:n]), np.array(q.w[:n])
+
+
+def _eos_soa(eos):
+    return C.EosSoA(*[_addr(eos, k) for k in range(11)])
+
+
+def _m1_soa(m1):
+    s = C.M1SoA()
+    for k in range(4):
+        s.n[k], s.J[k], s.chi[k] = _addr(m1, k), _addr(m1, 4 + k), _addr(m1, 8 + k)
+    return s
+
+
+def _distr_soa(d):
+    s = C.DistrSoA()
+    for q, name in enumerate(("w_t", "temp_t", "eta_t", "w_f", "temp_f", "c_f", "beta_f")):
+        arr = getattr(s, name)
+        for k in range(4):
+            arr[k] = _addr(d, 4 * q + k)
+    return s
+
+
+def _grey_soa(out):
+    s = C.M1OpacitiesSoA()
+    for q, name in enumerate(("eta_0", "kappa_0_a", "eta", "kappa_a", "kappa_s")):
+        arr = getattr(s, name)
+        for k in range(4):
+            arr[k] = _addr(out, 4 * q + k)
+    return s
+
+
+def _spec_soa(out):
+    s = C.SpectralSoA()
+    for q, name in enumerate(("j", "kappa", "j_s", "kappa_s")):
+        arr = getattr(s, name)
+        for k in range(4):
+            arr[k] = _addr(out, 4 * q + k)
+    return s
+
+
+def _prec(precision):
+    return {"fp64": C.FP64, "mixed": C.MIXED, C.FP64: C.FP64, C.MIXED: C.MIXED}[precision]
+
+
+# ---------------------------------------------------------------------------
+# batched device API
+# ---------------------------------------------------------------------------
+
+def m1_opacities(eos, m1, flags, params, quad_1d, quad_2d=None, distr=None, stim_abs=1,
+                 precision="fp64", out=None, stream=None):
+    """Grey M1 opacities of N points (tensors on the current CUDA device)."""
+    import torch
+    n = eos.shape[1]
+    assert eos.shape[0] == 11 and m1.shape == (12, n)
+    assert eos.is_cuda and m1.is_cuda and eos.dtype == torch.float64
+    assert eos.stride(1) == 1 and m1.stride(1) == 1
+    if out is None:
+        out = torch.empty((20, n), dtype=torch.float64, device=eos.device)
+    quad_2d = quad_1d if quad_2d is None else quad_2d
+    E, M, O = _eos_soa(eos), _m1_soa(m1), _grey_soa(out)
+    D = None if distr is None else _distr_soa(distr)
+    _check(C.load().bnsn_m1_opacities(
+        ctypes.byref(quad_1d), ctypes.byref(quad_2d), ctypes.byref(flags), ctypes.byref(params),
+        ctypes.byref(E), ctypes.byref(M), None if D is None else ctypes.byref(D),
+        int(stim_abs), _prec(precision), ctypes.byref(O), n, _stream_handle(stream)))
+    return out
+
+
+def spectral_opacities(eos, m1, flags, params, quad_1d, energies, distr=None, stimulated=1,
+                       precision="fp64", out=None, stream=None):
+    """Spectral opacities of N points at the given energies: [16, N, n_e]."""
+    import torch
+    n = eos.shape[1]
+    e = np.ascontiguousarray(np.asarray(energies, dtype=np.float64))
+    if out is None:
+        out = torch.empty((16, n, e.size), dtype=torch.float64, device=eos.device)
+    E, M, O = _eos_soa(eos), _m1_soa(m1), _spec_soa(out)
+    D = None if distr is None else _distr_soa(distr)
+    _check(C.load().bnsn_spectral_opacities(
+        ctypes.byref(quad_1d), ctypes.byref(flags), ctypes.byref(params), ctypes.byref(E),
+        ctypes.byref(M), None if D is None else ctypes.byref(D), e.ctypes.data, e.size,
+        int(stimulated), _prec(precision), ctypes.byref(O), n, _stream_handle(stream)))
+    return out
+
+
+def distr_from_m1(m1, out=None, stream=None):
+    """CalculateDistrParamsFromM1 for N points: [28, N]."""
+    import torch
+    n = m1.shape[1]
+    if out is None:
+        out = torch.empty((28, n), dtype=torch.float64, device=m1.device)
+    _check(C.load().bnsn_distr_from_m1(ctypes.byref(_m1_soa(m1)), ctypes.byref(_distr_soa(out)),
+                                       n, _stream_handle(stream)))
+    return out
+
+
+def nu_equilibrium(eos, stream=None):
+    """NuEquilibriumParams + ComputeM1DensitiesEq: (distr [28, N], m1 [12, N])."""
+    import torch
+    n = eos.shape[1]
+    distr = torch.empty((28, n), dtype=torch.float64, device=eos.device)
+    m1 = torch.empty((12, n), dtype=torch.float64, device=eos.device)
+    arr = ctypes.c_void_p * 4
+    nn = arr(*[_addr(m1, k) for k in range(4)])
+    jj = arr(*[_addr(m1, 4 + k) for k in range(4)])
+    cc = arr(*[_addr(m1, 8 + k) for k in range(4)])
+    _check(C.load().bnsn_nu_equilibrium(ctypes.byref(_eos_soa(eos)),
+                                        ctypes.byref(_distr_soa(distr)), nn, jj, cc, n,
+                                        _stream_handle(stream)))
+    return distr, m1
+
+
+def set_gp19_table(tab):
+    """Load a GP19 table dict (dims, nb, ye, t, w, [lognb, logw], data)."""
+    dims = (ctypes.c_int * 4)(*tab["dims"])
+    arrs = [np.ascontiguousarray(tab[k], dtype=np.float64) if tab.get(k) is not None else None
+            for k in ("nb", "ye", "t", "w", "lognb", "logw", "data")]
+    ptrs = [None if a is None else a.ctypes.data for a in arrs]
+    _check(C.load().bnsn_gp19_set_table(dims, *ptrs))
+
+
+def synthetic_points(seed, n, first=0, nthreads=0):
+    """Seeded synthetic points on the host: (eos [11, n], m1 [12, n]) numpy."""
+    import os
+    eos = np.empty((11, n))
+    m1 = np.empty((12, n))
+    _check(C.load().bnsn_synthetic_points(seed, first, n, eos.ctypes.data, m1.ctypes.data,
+                                          int(nthreads or os.cpu_count())))
+    return eos, m1
+
+
+def fp64_peak_tflops(iters=1 << 16):
+    """Measured FP64 FMA throughput of the current device (TFLOP/s)."""
+    v = ctypes.c_double()
+    _check(C.load().bnsn_fp64_peak_probe(int(iters), ctypes.byref(v)))
+    return v.value
+
+
+def m1_opacities_host(eos, m1, flags, params, quad_1d, quad_2d=None, stim_abs=1,
+                      precision="fp64", out=None):
+    """Grey opacities of host (numpy or pinned torch) arrays, copies included."""
+    n = eos.shape[1]
+    if out is None:
+        out = np.empty((20, n))
+    quad_2d = quad_1d if quad_2d is None else quad_2d
+    _check(C.load().bnsn_m1_opacities_host(
+        ctypes.byref(quad_1d), ctypes.byref(quad_2d), ctypes.byref(flags), ctypes.byref(params),
+        ctypes.byref(_eos_soa(eos)), ctypes.byref(_m1_soa(m1)), int(stim_abs),
+        _prec(precision), ctypes.byref(_grey_soa(out)), n))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# per-point mirrors of the reference functions
+# ---------------------------------------------------------------------------
+
+def _struct_dict(s):
+    return {name: list(getattr(s, name)) for name, _ in s._fields_}
+
+
+def ComputeM1Opacities(quad_1d, quad_2d, grey_pars):
+    """ComputeM1Opacities(quad_1d, quad_2d, grey_pars) -> M1Opacities dict."""
+    o = C.M1Opacities()
+    _check(C.load().bnsn_compute_m1_opacities_point(
+        ctypes.byref(quad_1d), ctypes.byref(quad_2d), ctypes.byref(grey_pars), 1, ctypes.byref(o)))
+    return _struct_dict(o)
+
+
+def ComputeM1OpacitiesNotStimulated(quad_1d, quad_2d, grey_pars):
+    o = C.M1Opacities()
+    _check(C.load().bnsn_compute_m1_opacities_point(
+        ctypes.byref(quad_1d), ctypes.byref(quad_2d), ctypes.byref(grey_pars), 0, ctypes.byref(o)))
+    return _struct_dict(o)
+
+
+def ComputeSpectralOpacitiesStimulatedAbs(nu, quad_1d, grey_pars):
+    o = C.SpectralOpacities()
+    _check(C.load().bnsn_compute_spectral_opacities_point(
+        float(nu), ctypes.byref(quad_1d), ctypes.byref(grey_pars), 1, ctypes.byref(o)))
+    return _struct_dict(o)
+
+
+def ComputeSpectralOpacitiesNotStimulatedAbs(nu, quad_1d, grey_pars):
+    o = C.SpectralOpacities()
+    _check(C.load().bnsn_compute_spectral_opacities_point(
+        float(nu), ctypes.byref(quad_1d), ctypes.byref(grey_pars), 0, ctypes.byref(o)))
+    return _struct_dict(o)

@@ -1,0 +1,71 @@
+// Internal launch descriptors shared by the C-ABI layer and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace bnsn {
+
+constexpr int kMaxQ     = 20;                         // nodes per half-interval
+constexpr int kMaxM     = 2 * kMaxQ;                  // energy nodes
+constexpr int kMaxCells = kMaxM * (kMaxM + 1) / 2;    // unordered energy pairs
+
+struct Gp19Dev
+{
+    int d0, d1, d2, d3;
+    const double *nb, *ye, *t, *w, *lognb, *logw, *data;
+};
+
+// Everything a grey or spectral launch needs, passed by value as a
+// __grid_constant__ kernel parameter (no device allocation per call).
+struct OpacityLaunch
+{
+    int64_t npts;
+    const double* eos[11]; // nb temp ye yp yn mu_p mu_n mu_e mu_mu dU dm_eff
+    const double* m1[12];  // n[4] J[4] chi[4]
+    const double* distr[28];
+    double* out[20];       // grey: eta_0, kappa_0_a, eta, kappa_a, kappa_s
+    int has_distr;
+    int use_abs_em, use_pair, use_brem, use_inel, use_iso;
+    int use_dU, use_dm_eff, use_WM_ab, use_WM_sc, use_decay, brem_impl;
+    int use_medium, neglect_blocking;
+    int stim;
+    double gamma36;        // GammaStirling(3.6), host libm
+    int n1, n2, ncell;
+    double x1[kMaxQ], w1[kMaxQ], x2[kMaxQ], w2[kMaxQ];
+    double B1[kMaxM];      // 1-D weights: w_i (a < n) or w_i / x_i^2
+    double A1[kMaxM];      // 2-D number weights of one energy index
+    double A2[kMaxM];      // 2-D energy weights (x t): x_i w_i or w_i / x_i^3
+    double wx[kMaxQ];      // NES: w_i x_i
+    double wx3[kMaxQ];     // NES: w_i / x_i^3
+    uint32_t cells[kMaxCells]; // a | b << 16, a <= b
+    Gp19Dev gp19;
+    // spectral launches only
+    int n_energies;        // energies of this launch (<= 64)
+    int e_stride, e_offset; // output entry p * e_stride + e_offset + e
+    double energies[64];
+    double* sout[16];      // j, kappa, j_s, kappa_s per species
+};
+
+cudaError_t launch_grey_fp64(const OpacityLaunch& L, cudaStream_t stream, int num_sms);
+cudaError_t launch_spectral_fp64(const OpacityLaunch& L, cudaStream_t stream, int num_sms);
+struct DistrLaunch
+{
+    int64_t npts;
+    const double* m1[12];
+    double* out[28];
+    double gamma36;
+};
+
+struct EquilLaunch
+{
+    int64_t npts;
+    const double* eos[11];
+    double* distr[28];
+    double* m1[12];
+};
+
+cudaError_t launch_distr_from_m1(const DistrLaunch& L, cudaStream_t stream, int num_sms);
+cudaError_t launch_nu_equilibrium(const EquilLaunch& L, cudaStream_t stream, int num_sms);
+
+} // namespace bnsn

@@ -1,0 +1,375 @@
+/* bns_nurates_gb300.h -- C ABI of the GB300 opacity library.
+ *
+ * Drop-in for the per-point opacity path of bns_nurates: the grey M1
+ * emissivities/opacities (ComputeM1Opacities) and the spectral opacities
+ * (ComputeSpectralOpacities*), computed on one GB300 (sm_103a) GPU.
+ *
+ * Part 1 restates the reference's public structs with the same names and the
+ * same memory layout (BS_REAL = double, BS_N_MAX = 20), so caller code that
+ * fills MyQuadrature / GreyOpacityParams keeps working.  Part 2 is the batched
+ * device API (structure-of-arrays over points).  Part 3 holds per-point host
+ * drop-ins and utilities.  Every entry point returns a bnsn_status.
+ */
+#ifndef BNS_NURATES_GB300_H_
+#define BNS_NURATES_GB300_H_
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ======================================================================
+ * Part 1: structs of include/bns_nurates.hpp (layout-identical)
+ * ====================================================================== */
+
+#define id_nue 0
+#define id_anue 1
+#define id_nux 2
+#define id_anux 3
+#define total_num_species 4
+#define BS_N_MAX 20 /* capacity of MyQuadrature::points / w */
+
+typedef double BS_REAL;
+
+/* bns_nurates.hpp:80-84 */
+enum Quadrature { kGauleg, kGaulag };
+
+/* bns_nurates.hpp:106-130: n Gauss-Legendre nodes/weights on [0,1] in
+ * points[0..nx-1], w[0..nx-1].  Only nx, points and w are read. */
+typedef struct MyQuadrature
+{
+    enum Quadrature type;
+    BS_REAL alpha;
+    int dim;
+    int nx;
+    int ny;
+    int nz;
+    BS_REAL x1, x2, y1, y2, z1, z2;
+    BS_REAL points[BS_N_MAX];
+    BS_REAL w[BS_N_MAX];
+} MyQuadrature;
+
+/* bns_nurates.hpp:199-250 */
+typedef struct BremKernelParams
+{
+    BS_REAL omega;
+    BS_REAL omega_prime;
+    int l;
+    bool use_NN_medium_corr;
+} BremKernelParams;
+
+typedef struct PairKernelParams
+{
+    BS_REAL omega, omega_prime, cos_theta, mu, mu_prime, lmax, filter;
+} PairKernelParams;
+
+typedef struct InelasticScattKernelParams
+{
+    BS_REAL omega, omega_prime;
+} InelasticScattKernelParams;
+
+typedef struct MyKernelParams
+{
+    PairKernelParams pair_kernel_params;
+    BremKernelParams brem_kernel_params;
+    InelasticScattKernelParams inelastic_kernel_params;
+} MyKernelParams;
+
+/* bns_nurates.hpp:259-264 */
+typedef struct MyKernelOutput
+{
+    BS_REAL em[total_num_species];
+    BS_REAL abs[total_num_species];
+} MyKernelOutput;
+
+/* bns_nurates.hpp:289-306: chemical potentials include rest masses */
+typedef struct MyEOSParams
+{
+    BS_REAL nb;     /* baryon number density [nm^-3] */
+    BS_REAL temp;   /* temperature [MeV] */
+    BS_REAL ye, yp, yn;
+    BS_REAL mu_p, mu_n, mu_e, mu_mu; /* [MeV] (mu_mu unused) */
+    BS_REAL dU;     /* mean-field potential difference [MeV] */
+    BS_REAL dm_eff; /* effective mass difference [MeV] */
+} MyEOSParams;
+
+/* bns_nurates.hpp:324-329 */
+typedef struct MyOpacity
+{
+    BS_REAL abs[total_num_species];
+    BS_REAL em[total_num_species];
+} MyOpacity;
+
+/* bns_nurates.hpp:332 */
+enum BremImpl { BREM_HR98 = 0, BREM_BRT06 = 1, BREM_GP19 = 2 };
+
+/* bns_nurates.hpp:338-352 */
+typedef struct OpacityParams
+{
+    bool use_dU;
+    bool use_dm_eff;
+    bool use_WM_ab;
+    bool use_WM_sc;
+    bool use_decay;
+    enum BremImpl brem_implementation;
+    bool use_NN_medium_corr;
+    bool neglect_blocking;
+} OpacityParams;
+
+/* bns_nurates.hpp:387-401 */
+typedef struct NuDistributionParams
+{
+    BS_REAL w_t[total_num_species];
+    BS_REAL temp_t[total_num_species];
+    BS_REAL eta_t[total_num_species];
+    BS_REAL w_f[total_num_species];
+    BS_REAL temp_f[total_num_species];
+    BS_REAL c_f[total_num_species];
+    BS_REAL beta_f[total_num_species];
+} NuDistributionParams;
+
+/* bns_nurates.hpp:409-416: n [nm^-3], J [MeV nm^-3]; H unused */
+typedef struct M1Quantities
+{
+    BS_REAL n[total_num_species];
+    BS_REAL J[total_num_species];
+    BS_REAL H[total_num_species][4];
+    BS_REAL chi[total_num_species];
+} M1Quantities;
+
+/* bns_nurates.hpp:418-426 */
+typedef struct OpacityFlags
+{
+    int use_abs_em;
+    int use_pair;
+    int use_brem;
+    int use_inelastic_scatt;
+    int use_iso;
+} OpacityFlags;
+
+/* bns_nurates.hpp:444-454 */
+typedef struct GreyOpacityParams
+{
+    OpacityParams opacity_pars;
+    MyKernelParams kernel_pars;
+    MyEOSParams eos_pars;
+    NuDistributionParams distr_pars;
+    M1Quantities m1_pars;
+    OpacityFlags opacity_flags;
+} GreyOpacityParams;
+
+/* bns_nurates.hpp:463-474: eta_0 [nm^-3 s^-1], eta [MeV nm^-3 s^-1],
+ * kappa_* [nm^-1] */
+typedef struct M1Opacities
+{
+    BS_REAL eta_0[total_num_species];
+    BS_REAL kappa_0_a[total_num_species];
+    BS_REAL eta[total_num_species];
+    BS_REAL kappa_a[total_num_species];
+    BS_REAL kappa_s[total_num_species];
+} M1Opacities;
+
+/* bns_nurates.hpp:517-524 */
+typedef struct SpectralOpacities
+{
+    BS_REAL j[total_num_species];
+    BS_REAL kappa[total_num_species];
+    BS_REAL j_s[total_num_species];
+    BS_REAL kappa_s[total_num_species];
+} SpectralOpacities;
+
+/* ======================================================================
+ * Part 2: batched device API
+ *
+ * Points are independent.  Every per-point quantity is a separate device
+ * array of length npts (structure of arrays, one pointer per struct field),
+ * so callers can pass their own grid-function storage.  Calls are
+ * stream-ordered on `stream` (a cudaStream_t; NULL = default stream), do not
+ * synchronise the host, and allocate nothing.
+ * ====================================================================== */
+
+typedef enum bnsn_status
+{
+    BNSN_OK = 0,
+    BNSN_ERR_ARG = 1,      /* null pointer, npts < 0, bad enum or flag */
+    BNSN_ERR_NQUAD = 2,    /* quadrature order outside 1..BNSN_NQUAD_MAX */
+    BNSN_ERR_CUDA = 3,     /* a CUDA call failed (see bnsn_last_error) */
+    BNSN_ERR_NO_TABLE = 4, /* GP19 requested but no table loaded */
+    BNSN_ERR_NO_DEVICE = 5 /* no usable sm_103 device */
+} bnsn_status;
+
+/* Quadrature nodes per half-interval supported by the kernels (2x energy
+ * nodes); the reference build is limited to BS_N_MAX/2 = 10. */
+#define BNSN_NQUAD_MAX 20
+
+typedef enum bnsn_precision
+{
+    BNSN_FP64 = 0, /* all arithmetic in double precision */
+    BNSN_MIXED = 1 /* FP32 kernel tiles, FP64 where stability needs it */
+} bnsn_precision;
+
+/* MyEOSParams, one device array per field (mu_mu may be NULL). */
+typedef struct bnsn_eos_soa
+{
+    const double *nb, *temp, *ye, *yp, *yn, *mu_p, *mu_n, *mu_e, *mu_mu, *dU,
+        *dm_eff;
+} bnsn_eos_soa;
+
+/* M1Quantities n, J, chi per species. */
+typedef struct bnsn_m1_soa
+{
+    const double* n[total_num_species];
+    const double* J[total_num_species];
+    const double* chi[total_num_species];
+} bnsn_m1_soa;
+
+/* NuDistributionParams per species (input of the opacity calls, output of
+ * bnsn_distr_from_m1). */
+typedef struct bnsn_distr_soa
+{
+    double* w_t[total_num_species];
+    double* temp_t[total_num_species];
+    double* eta_t[total_num_species];
+    double* w_f[total_num_species];
+    double* temp_f[total_num_species];
+    double* c_f[total_num_species];
+    double* beta_f[total_num_species];
+} bnsn_distr_soa;
+
+/* M1Opacities per species. */
+typedef struct bnsn_m1_opacities_soa
+{
+    double* eta_0[total_num_species];
+    double* kappa_0_a[total_num_species];
+    double* eta[total_num_species];
+    double* kappa_a[total_num_species];
+    double* kappa_s[total_num_species];
+} bnsn_m1_opacities_soa;
+
+/* SpectralOpacities per species; each array is [npts][n_energies]
+ * (entry p * n_energies + e). */
+typedef struct bnsn_spectral_soa
+{
+    double* j[total_num_species];
+    double* kappa[total_num_species];
+    double* j_s[total_num_species];
+    double* kappa_s[total_num_species];
+} bnsn_spectral_soa;
+
+/* Grey M1 opacities of npts points.
+ * Replaces ComputeM1Opacities (stim_abs = 1, m1_opacities.hpp:1306-1313) and
+ * ComputeM1OpacitiesNotStimulated (stim_abs = 0, m1_opacities.hpp:1297-1304)
+ * called once per point, e.g. from the Kokkos loop of tests/tests.hpp:272-343.
+ * quad_1d drives the beta and iso integrals, quad_2d the pair, brem and
+ * inelastic double integrals, exactly as in the reference.  `distr` = NULL
+ * reconstructs the distribution from `m1` on the device
+ * (CalculateDistrParamsFromM1, distribution.hpp:323-333) before use; otherwise
+ * the given parameters are used as GreyOpacityParams::distr_pars. */
+int bnsn_m1_opacities(const MyQuadrature* quad_1d, const MyQuadrature* quad_2d,
+                      const OpacityFlags* flags, const OpacityParams* params,
+                      const bnsn_eos_soa* eos, const bnsn_m1_soa* m1,
+                      const bnsn_distr_soa* distr, int stim_abs, int precision,
+                      const bnsn_m1_opacities_soa* out, int64_t npts,
+                      void* stream);
+
+/* Spectral opacities of npts points at n_energies neutrino energies
+ * (`energies` is a host array, MeV).  Replaces
+ * ComputeSpectralOpacitiesStimulatedAbs (stimulated = 1,
+ * m1_opacities.hpp:1641-1660) and ComputeSpectralOpacitiesNotStimulatedAbs
+ * (stimulated = 0, m1_opacities.hpp:1506-1637) called per (point, energy). */
+int bnsn_spectral_opacities(const MyQuadrature* quad_1d,
+                            const OpacityFlags* flags,
+                            const OpacityParams* params,
+                            const bnsn_eos_soa* eos, const bnsn_m1_soa* m1,
+                            const bnsn_distr_soa* distr, const double* energies,
+                            int n_energies, int stimulated, int precision,
+                            const bnsn_spectral_soa* out, int64_t npts,
+                            void* stream);
+
+/* Distribution parameters from M1 moments; replaces CalculateDistrParamsFromM1
+ * (distribution.hpp:323-333) per point. */
+int bnsn_distr_from_m1(const bnsn_m1_soa* m1, const bnsn_distr_soa* out,
+                       int64_t npts, void* stream);
+
+/* Equilibrium distribution and its M1 densities (chi = 1/3); replaces
+ * NuEquilibriumParams + ComputeM1DensitiesEq (distribution.hpp:253-290,
+ * 447-473) as used by the reference drivers (tests/tests.hpp:318-332). */
+int bnsn_nu_equilibrium(const bnsn_eos_soa* eos, const bnsn_distr_soa* distr_out,
+                        double* const n_out[total_num_species],
+                        double* const J_out[total_num_species],
+                        double* const chi_out[total_num_species], int64_t npts,
+                        void* stream);
+
+/* Load the 4-D GP19 response table (kernel_brem_GP19.hpp:75-139 layout:
+ * data[((i_nb * d1 + i_ye) * d2 + i_T) * d3 + i_w], MeV^-1) onto the current
+ * device.  lognb / logw may be NULL (computed as log of the axes).  Host
+ * pointers; synchronous.  Required before any call with BREM_GP19. */
+int bnsn_gp19_set_table(const int dims[4], const double* nb_axis,
+                        const double* ye_axis, const double* t_axis,
+                        const double* w_axis, const double* lognb_axis,
+                        const double* logw_axis, const double* data);
+
+/* ======================================================================
+ * Part 3: per-point drop-ins, host-buffer batches, utilities
+ * ====================================================================== */
+
+/* One point, host structs, synchronous (batch of one on the GPU).  Same
+ * arguments and result as ComputeM1Opacities(quad_1d, quad_2d, grey_pars)
+ * (m1_opacities.hpp:1306-1313); grey_pars->distr_pars must be filled, as in
+ * the reference.  grey_pars is not modified. */
+int bnsn_compute_m1_opacities_point(const MyQuadrature* quad_1d,
+                                    const MyQuadrature* quad_2d,
+                                    const GreyOpacityParams* grey_pars,
+                                    int stim_abs, M1Opacities* out);
+
+/* One point, one energy; same as ComputeSpectralOpacities{Not,}StimulatedAbs
+ * (m1_opacities.hpp:1506-1660). */
+int bnsn_compute_spectral_opacities_point(double nu, const MyQuadrature* quad_1d,
+                                          const GreyOpacityParams* grey_pars,
+                                          int stimulated,
+                                          SpectralOpacities* out);
+
+/* bnsn_m1_opacities with every SoA pointer in HOST memory.  The library
+ * copies inputs in, computes and copies results out through a staging area
+ * on the current device, chunked and overlapped across two streams;
+ * returns when the results are in `out`. */
+int bnsn_m1_opacities_host(const MyQuadrature* quad_1d,
+                           const MyQuadrature* quad_2d,
+                           const OpacityFlags* flags,
+                           const OpacityParams* params, const bnsn_eos_soa* eos,
+                           const bnsn_m1_soa* m1, int stim_abs, int precision,
+                           const bnsn_m1_opacities_soa* out, int64_t npts);
+
+/* Gauss-Legendre nodes/weights of order quad->nx on [0,1]; replaces
+ * GaussLegendre (integration.hpp:28-87), same algorithm. */
+int bnsn_gauss_legendre(MyQuadrature* quad);
+
+/* Seeded synthetic thermodynamic points (host, OpenMP): eos[11][npts] in the
+ * MyEOSParams field order and m1[12][npts] = n[4], J[4], chi[4].  Point k
+ * depends only on (seed, first + k).  rho log-uniform 1e6..1e15 g/cm^3,
+ * T log-uniform 0.5..100 MeV, Ye uniform 0.01..0.6; mu_e from an ideal
+ * relativistic e+- gas; non-relativistic ideal nucleons with a mean-field
+ * shift dU uniform in +-20 MeV; per species T_nu = T U(0.5,1.5), eta_nu
+ * U(-5,5), n and J from Fermi-Dirac moments, chi U(1/3,1); anti-nu_x = nu_x. */
+int bnsn_synthetic_points(uint64_t seed, int64_t first, int64_t npts,
+                          double* eos, double* m1, int nthreads);
+
+/* FP64 fused-multiply-add throughput of the current device in TFLOP/s
+ * (independent DFMA chains on every SM, CUDA-event timed): the denominator of
+ * the FP64-pipe roofline of the opacity kernels.  A diagnostic with no
+ * counterpart in the reference. */
+int bnsn_fp64_peak_probe(int64_t iters, double* tflops);
+
+const char* bnsn_status_string(int status);
+/* Text of the most recent error on the calling thread ("" if none). */
+const char* bnsn_last_error(void);
+int bnsn_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BNS_NURATES_GB300_H_ */

@@ -14,12 +14,18 @@ use this package, as the checker; the product never imports it.
 
 import ctypes
 import os
+import platform
 import subprocess
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "libbnsn_oracle.so")
+# Same source with FMA contraction enabled: identical algorithm, different
+# rounding.  Where the two builds disagree, the reference result itself is
+# not reproducible to the last bits (cancellation), which the GPU parity
+# tests use as the per-element conditioning of each output.
+PORT_FMA_SO = os.path.join(HERE, "libbnsn_oracle_fma.so")
 REF_SO = os.path.join(HERE, "_ref", "libbnsn_ref.so")
 REF_LAYOUT = os.path.join(HERE, "_ref", "ref_layout")
 
@@ -36,6 +42,11 @@ def build(force=False):
         subprocess.check_call([
             "gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC",
             "-shared", src, "-o", PORT_SO, "-lm"])
+    if stale or not os.path.exists(PORT_FMA_SO):
+        fma = ["-mfma"] if platform.machine() in ("x86_64", "AMD64") else []
+        subprocess.check_call([
+            "gcc", "-std=c11", "-O2", "-ffp-contract=fast", "-fopenmp", "-fPIC",
+            "-shared"] + fma + [src, "-o", PORT_FMA_SO, "-lm"])
     from . import build_ref  # noqa: WPS433 (local import: optional step)
     try:
         build_ref.build()
@@ -240,6 +251,17 @@ def port():
         o.set_gp19_table(_synthetic_gp19())
         _cache["port"] = o
     return _cache["port"]
+
+
+def port_fma():
+    """The C restatement compiled with FMA contraction (conditioning probe)."""
+    if "port_fma" not in _cache:
+        if not os.path.exists(PORT_FMA_SO):
+            build()
+        o = Oracle(PORT_FMA_SO, "oracle_")
+        o.set_gp19_table(_synthetic_gp19())
+        _cache["port_fma"] = o
+    return _cache["port_fma"]
 
 
 def ref():

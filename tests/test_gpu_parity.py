@@ -1,0 +1,285 @@
+"""Parity of the FP64 GPU path with the CPU oracle and the reference.
+
+Calls go through the C ABI (ctypes), inputs and outputs live in device memory
+allocated by torch.
+
+Tolerance.  The plain path's contract is 1e-12 relative per emissivity and
+opacity.  The reference's own result is not reproducible to that level
+everywhere: recompiling the same C restatement with FMA contraction (same
+algorithm, different rounding) moves some outputs by up to ~1e-6, in the
+cancellation-dominated pair/NES terms of degenerate matter.  Each element's
+sensitivity to O(eps) perturbations is estimated from three probes of the
+oracle: the FMA build, and the plain build with the temperature and with the
+electron chemical potential moved by two ulps.  Its tolerance is
+max(1e-12, COND x largest probe deviation): 1e-12 wherever the reference is
+well conditioned, and the reference's own sensitivity (times a safety factor)
+where it is not.
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+import bns_nurates_gb300 as bn
+from conftest import golden, rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+COND = 64.0
+NTHREADS = os.cpu_count()
+
+
+@pytest.fixture(scope="module")
+def port_fma():
+    import oracle
+    return oracle.port_fma()
+
+
+def P(*vals):
+    return bn.opacity_params(*[bool(v) for v in vals[:5]], brem_implementation=int(vals[5]),
+                             use_NN_medium_corr=bool(vals[6]), neglect_blocking=bool(vals[7]))
+
+
+def F(vals):
+    return bn.opacity_flags(*vals)
+
+
+def gpu_grey(torch, eos, m1, flags, pars, nq, stim=1, distr=None, nq1=None):
+    q2 = bn.gauss_legendre(nq)
+    q1 = q2 if nq1 is None else bn.gauss_legendre(nq1)
+    e = torch.from_numpy(np.ascontiguousarray(eos)).cuda()
+    m = torch.from_numpy(np.ascontiguousarray(m1)).cuda()
+    d = None if distr is None else torch.from_numpy(np.ascontiguousarray(distr)).cuda()
+    out = bn.m1_opacities(e, m, F(flags), P(*pars), q1, q2, distr=d, stim_abs=stim)
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def oracle_grey(port, eos, m1, flags, pars, nq, stim=1, distr=None, nq1=None):
+    q2 = port.gauss_legendre(nq)
+    q1 = q2 if nq1 is None else port.gauss_legendre(nq1)
+    return port.m1_opacities(eos, m1, flags, pars, q1, q2, distr=distr, stim_abs=stim,
+                             nthreads=NTHREADS)
+
+
+def _bumped(eos, row):
+    e = np.array(eos, dtype=np.float64, copy=True)
+    e[row] = e[row] * (1. + 2. ** -51)
+    return e
+
+
+def probes(fn, fma_fn, eos, *args, **kw):
+    """Oracle results under three O(eps) perturbations (FMA rounding, +2 ulp in
+    T, +2 ulp in mu_e), to estimate each element's conditioning."""
+    return [fma_fn(eos, *args, **kw), fn(_bumped(eos, 1), *args, **kw),
+            fn(_bumped(eos, 7), *args, **kw)]
+
+
+def grey_probes(port, port_fma, eos, *args, **kw):
+    return probes(lambda e, *a, **k: oracle_grey(port, e, *a, **k),
+                  lambda e, *a, **k: oracle_grey(port_fma, e, *a, **k), eos, *args, **kw)
+
+
+def assert_close(got, want, perturbed=None, what=""):
+    """|got - want| <= max(TOL, COND * max_k |want - perturbed_k|) * |want|."""
+    r = rel_err(got, want, floor=1e-300)
+    tol = np.full(r.shape, TOL)
+    for alt in (perturbed or []):
+        tol = np.maximum(tol, COND * rel_err(alt, want, floor=1e-300))
+    assert (np.isfinite(got) == np.isfinite(want)).all(), f"{what}: finiteness differs"
+    bad = r > tol
+    if bad.any():
+        k = np.unravel_index(np.argmax(r / tol), r.shape)
+        raise AssertionError(f"{what}: {bad.sum()} of {r.size} elements out of tolerance; "
+                             f"worst {k}: rel err {r[k]:.3e}, tol {tol[k]:.3e}")
+    return r
+
+
+DEFAULT = (1, 0, 1, 1, 1, 0, 1, 0)   # dU, no dm_eff, WM ab/sc, decay, HR98, medium corr
+
+
+def test_constants_and_fdi_via_point_api(cuda, port):
+    """A single point through the per-point drop-in equals the oracle."""
+    g = golden("point_a.npz")
+    gp = bn.GreyOpacityParams()
+    names = ("nb", "temp", "ye", "yp", "yn", "mu_p", "mu_n", "mu_e", "mu_mu", "dU", "dm_eff")
+    for k, nme in enumerate(names):
+        setattr(gp.eos_pars, nme, float(g["eos"][k, 0]))
+    for s in range(4):
+        gp.m1_pars.n[s] = g["m1"][s, 0]
+        gp.m1_pars.J[s] = g["m1"][4 + s, 0]
+        gp.m1_pars.chi[s] = g["m1"][8 + s, 0]
+    d = port.distr_from_m1(g["eos"], g["m1"])[:, 0]
+    for q, nme in enumerate(("w_t", "temp_t", "eta_t", "w_f", "temp_f", "c_f", "beta_f")):
+        for s in range(4):
+            getattr(gp.distr_pars, nme)[s] = d[4 * q + s]
+    gp.opacity_flags = F((1, 1, 1, 1, 1))
+    gp.opacity_pars = P(*g["pars"])
+    q = bn.gauss_legendre(6)
+    o = bn.ComputeM1Opacities(q, q, gp)
+    got = np.array([o[k] for k in ("eta_0", "kappa_0_a", "eta", "kappa_a", "kappa_s")]).ravel()
+    qo = (g["x"], g["w"])
+    pfma = __import__("oracle").port_fma()
+    pr = [p[:, 0] for p in probes(port.m1_opacities, pfma.m1_opacities, g["eos"], g["m1"],
+                                   (1, 1, 1, 1, 1), g["pars"], qo)]
+    assert_close(got, g["out"][:, 0], pr, what="point A grey")
+    s = bn.ComputeSpectralOpacitiesNotStimulatedAbs(10., q, gp)
+    got = np.array([s[k] for k in ("j", "kappa", "j_s", "kappa_s")]).ravel()
+    pr = [p[:, 0, 0] for p in probes(port.spectral, pfma.spectral, g["eos"], g["m1"],
+                                      (1, 1, 1, 1, 1), g["pars"], qo, np.array([10.]),
+                                      stimulated=0)]
+    assert_close(got, g["spec"][:, 0, 0], pr, what="point A spectral")
+
+
+@pytest.mark.parametrize("name", ["grey_hr98_n10.npz", "grey_all_hr98_n10.npz",
+                                  "grey_all_gp19_n20.npz", "grey_brt06_nostim.npz",
+                                  "grey_given_distr.npz"])
+def test_grey_vs_reference_golden(cuda, port_fma, name):
+    g = golden(name)
+    distr = g["distr"] if g["distr"].size else None
+    got = gpu_grey(cuda, g["eos"], g["m1"], g["flags"], g["pars"], len(g["x"]),
+                   stim=int(g["stim"]), distr=distr)
+    port = __import__("oracle").port()
+    pr = grey_probes(port, port_fma, g["eos"], g["m1"], g["flags"], g["pars"], len(g["x"]),
+                     stim=int(g["stim"]), distr=distr)
+    assert_close(got, g["out"], pr, what=name)
+
+
+def test_grey_c1_config_vs_oracle(cuda, port, port_fma):
+    """4096 synthetic points, beta + iso + pair + HR98, n = 10, FP64."""
+    eos, m1 = bn.synthetic_points(20261203, 4096)
+    flags = (1, 1, 1, 0, 1)
+    got = gpu_grey(cuda, eos, m1, flags, DEFAULT, 10)
+    want = oracle_grey(port, eos, m1, flags, DEFAULT, 10)
+    pr = grey_probes(port, port_fma, eos, m1, flags, DEFAULT, 10)
+    r = assert_close(got, want, pr, what="C1 grey")
+    # most elements are well conditioned and meet 1e-12 outright
+    assert (r <= TOL).mean() > 0.9
+
+
+@pytest.mark.parametrize("flags,pars,nq,nq1,stim", [
+    ((1, 1, 1, 1, 1), DEFAULT, 10, None, 1),
+    ((1, 1, 1, 1, 1), (1, 1, 1, 1, 1, 2, 1, 0), 20, None, 1),
+    ((1, 1, 1, 1, 1), (0, 0, 0, 0, 0, 1, 0, 1), 8, 12, 0),
+    ((0, 1, 0, 0, 0), DEFAULT, 5, None, 1),
+    ((0, 0, 1, 0, 0), (1, 0, 1, 1, 1, 2, 1, 0), 20, None, 0),
+    ((0, 0, 0, 1, 0), DEFAULT, 10, None, 1),
+    ((1, 0, 0, 0, 1), DEFAULT, 3, None, 0),
+])
+def test_grey_reaction_matrix_vs_oracle(cuda, port, port_fma, flags, pars, nq, nq1, stim):
+    eos, m1 = bn.synthetic_points(77, 384, first=nq * 100 + stim)
+    got = gpu_grey(cuda, eos, m1, flags, pars, nq, stim=stim, nq1=nq1)
+    want = oracle_grey(port, eos, m1, flags, pars, nq, stim=stim, nq1=nq1)
+    pr = grey_probes(port, port_fma, eos, m1, flags, pars, nq, stim=stim, nq1=nq1)
+    assert_close(got, want, pr, what=f"grey {flags} {pars} n={nq}")
+
+
+def test_spectral_vs_reference_golden(cuda, port_fma):
+    g = golden("spectral_n10.npz")
+    e = cuda.from_numpy(g["eos"]).cuda()
+    m = cuda.from_numpy(g["m1"]).cuda()
+    q = bn.gauss_legendre(10)
+    for stim in (0, 1):
+        out = bn.spectral_opacities(e, m, F(g["flags"]), P(*g["pars"]), q, g["energies"],
+                                    stimulated=stim)
+        cuda.cuda.synchronize()
+        port = __import__("oracle").port()
+        pr = probes(port.spectral, port_fma.spectral, g["eos"], g["m1"], g["flags"], g["pars"],
+                    (g["x"], g["w"]), g["energies"], stimulated=stim)
+        assert_close(out.cpu().numpy(), g[f"stim{stim}"], pr, what=f"spectral stim={stim}")
+
+
+@pytest.mark.parametrize("flags,pars,nq", [
+    ((1, 1, 1, 0, 1), DEFAULT, 10),
+    ((1, 1, 1, 1, 1), (1, 0, 1, 1, 1, 1, 0, 1), 7),
+    ((1, 1, 1, 1, 1), (1, 0, 1, 1, 1, 2, 1, 0), 20),
+])
+def test_spectral_vs_oracle(cuda, port, port_fma, flags, pars, nq):
+    eos, m1 = bn.synthetic_points(91, 48, first=nq)
+    energies = np.logspace(0., np.log10(300.), 24)
+    e = cuda.from_numpy(eos).cuda()
+    m = cuda.from_numpy(m1).cuda()
+    out = bn.spectral_opacities(e, m, F(flags), P(*pars), bn.gauss_legendre(nq), energies)
+    cuda.cuda.synchronize()
+    q = port.gauss_legendre(nq)
+    want = port.spectral(eos, m1, flags, pars, q, energies, nthreads=NTHREADS)
+    pr = probes(port.spectral, port_fma.spectral, eos, m1, flags, pars, q, energies,
+                nthreads=NTHREADS)
+    assert_close(out.cpu().numpy(), want, pr, what="spectral")
+
+
+def test_spectral_many_energies_chunked(cuda, port, port_fma):
+    """More than 64 energies are processed in chunks with the right layout."""
+    eos, m1 = bn.synthetic_points(5, 6)
+    energies = np.logspace(-1., 3., 100)
+    flags, pars = (1, 1, 1, 1, 1), DEFAULT
+    e, m = cuda.from_numpy(eos).cuda(), cuda.from_numpy(m1).cuda()
+    out = bn.spectral_opacities(e, m, F(flags), P(*pars), bn.gauss_legendre(4), energies)
+    cuda.cuda.synchronize()
+    q = port.gauss_legendre(4)
+    want = port.spectral(eos, m1, flags, pars, q, energies)
+    pr = probes(port.spectral, port_fma.spectral, eos, m1, flags, pars, q, energies)
+    assert_close(out.cpu().numpy(), want, pr, what="spectral 100 energies")
+
+
+def test_distr_and_equilibrium_vs_oracle(cuda, port):
+    eos, m1 = bn.synthetic_points(3, 2000)
+    m = cuda.from_numpy(m1).cuda()
+    got = bn.distr_from_m1(m).cpu().numpy()
+    assert_close(got, port.distr_from_m1(eos, m1), what="distr_from_m1")
+    d, mm = bn.nu_equilibrium(cuda.from_numpy(eos).cuda())
+    dw, mw = port.nu_equilibrium(eos)
+    assert_close(d.cpu().numpy(), dw, what="equilibrium distr")
+    assert_close(mm.cpu().numpy(), mw, what="equilibrium m1")
+
+
+def test_host_buffer_batch_equals_device_batch(cuda):
+    eos, m1 = bn.synthetic_points(4, 3000)
+    flags, pars = (1, 1, 1, 1, 1), DEFAULT
+    q = bn.gauss_legendre(10)
+    dev = gpu_grey(cuda, eos, m1, flags, pars, 10)
+    host = bn.m1_opacities_host(eos, m1, F(flags), P(*pars), q)
+    assert np.array_equal(dev, host)
+
+
+def test_deterministic_and_empty(cuda):
+    eos, m1 = bn.synthetic_points(6, 1000)
+    a = gpu_grey(cuda, eos, m1, (1, 1, 1, 1, 1), DEFAULT, 10)
+    b = gpu_grey(cuda, eos, m1, (1, 1, 1, 1, 1), DEFAULT, 10)
+    assert np.array_equal(a, b)
+    empty = gpu_grey(cuda, eos[:, :0], m1[:, :0], (1, 1, 1, 1, 1), DEFAULT, 10)
+    assert empty.shape == (20, 0)
+
+
+def test_gp19_requires_table(cuda):
+    """BREM_GP19 without a loaded table is an error, not zeros (the reference
+    device build silently returns 0, kernel_brem_GP19.hpp:483-491)."""
+    from bns_nurates_gb300 import _capi as C
+    lib = C.load()
+    import ctypes
+    # a fresh device state cannot be emulated in-process; check the error path
+    # through a status query instead: the table is loaded here, so the call works
+    eos, m1 = bn.synthetic_points(9, 64)
+    got = gpu_grey(cuda, eos, m1, (0, 0, 1, 0, 0), (1, 0, 1, 1, 1, 2, 1, 0), 6)
+    assert np.isfinite(got).all()
+    assert lib.bnsn_status_string(C.ERR_NO_TABLE) == b"GP19 table not loaded"
+    assert ctypes.sizeof(C.OpacityParams) == 12
+
+
+def test_full_size_subsample_parity(cuda, port, port_fma):
+    """128^3 = 2,097,152 points on the GPU; every 4096th point vs the oracle,
+    finiteness on all points, and chunk independence (a launch over a slice
+    gives the same bits as the full launch)."""
+    n = 128 ** 3
+    eos, m1 = bn.synthetic_points(20261203, n)
+    flags = (1, 1, 1, 0, 1)
+    got = gpu_grey(cuda, eos, m1, flags, DEFAULT, 10)
+    assert np.isfinite(got).all()
+    idx = np.arange(0, n, 4096)
+    want = oracle_grey(port, eos[:, idx], m1[:, idx], flags, DEFAULT, 10)
+    pr = grey_probes(port, port_fma, eos[:, idx], m1[:, idx], flags, DEFAULT, 10)
+    assert_close(got[:, idx], want, pr, what="128^3 subsample")
+    part = gpu_grey(cuda, eos[:, 1000:1000 + 4096], m1[:, 1000:1000 + 4096], flags, DEFAULT, 10)
+    assert np.array_equal(part, got[:, 1000:1000 + 4096])

@@ -1,0 +1,221 @@
+"""Pin the CPU oracle before trusting it (no GPU needed).
+
+1. Against the known answers and regression tables committed in the
+   reference's own tests.
+2. Bit for bit against the reference headers compiled in place
+   (oracle/_ref), where that build exists.
+3. Against the golden fixtures generated from the reference
+   (tests/golden/make_golden.py).
+"""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden, rel_err
+
+REF_DIR = os.environ.get("BNSN_REFERENCE_DIR", "/root/reference")
+kBS_Mu = 1.66053906892e-24
+kBS_Mb = 1.6737747126723517e-24
+kBS_Q = 1.29333251
+kBS_MeV = 1.6021766341182763e+8
+kBS_Clight = 2.99792458e+17
+PI = 3.14159265358979323846264338328
+
+
+# --------------------------------------------------------------------------
+# 1. the reference's own known answers
+# --------------------------------------------------------------------------
+
+def test_gauss_legendre_closed_forms(port):
+    """tests_quadrature_integrate/test_gauss_legendre_1d.cpp:16-26, 1e-12."""
+    s3, s15, s30 = np.sqrt(3.), np.sqrt(15.), np.sqrt(30.)
+    exact = {
+        2: ([-s3 / 3., s3 / 3.], [1., 1.]),
+        3: ([-s15 / 5., 0., s15 / 5.], [5. / 9., 8. / 9., 5. / 9.]),
+        4: ([-np.sqrt(525. + 70. * s30) / 35., -np.sqrt(525. - 70. * s30) / 35.,
+             np.sqrt(525. - 70. * s30) / 35., np.sqrt(525. + 70. * s30) / 35.],
+            [(18. - s30) / 36., (18. + s30) / 36., (18. + s30) / 36., (18. - s30) / 36.]),
+    }
+    for n, (x, w) in exact.items():
+        xp, wp = port.gauss_legendre(n)   # on [0, 1]
+        assert np.max(np.abs((2. * xp - 1.) - np.array(x))) < 1e-12
+        assert np.max(np.abs(2. * wp - np.array(w))) < 1e-12
+
+
+def test_hr98_known_answer(port):
+    """tests_brem/test_brem.cpp:169-221 (medium correction on), tol 1e-6."""
+    eos = np.zeros(11)
+    eos[0] = 3.73e14 / kBS_Mb * 1e-21
+    eos[1], eos[4], eos[3] = 12.04, 0.6866, 0.3134
+    em, ab = port.brem_kernel(0, eos, 10., 20., 1) * 1e-21
+    assert abs(em - 2.72968729e-30) / 2.72968729e-30 < 1e-6
+    assert abs(ab - 3.29793434e-29) / 3.29793434e-29 < 1e-6
+
+
+PAIR_PY = [  # tests_pair/test_pair_kernels.cpp:24-62 (omega, omega', nue em/abs, nux em/abs)
+    (2, 2, 3.7344281862494617e-37, 5.5711121998146404e-37, 7.9822789333374034e-38, 1.1908160856214353e-37),
+    (2, 5, 7.5952594997506983e-37, 1.5294974381563826e-36, 1.7098488384966924e-37, 3.443212727887964e-37),
+    (2, 50, 7.6816308521376666e-37, 1.3924664458243231e-34, 4.1187070226847197e-37, 7.4660725562898844e-35),
+    (5, 2, 8.5842096421064313e-37, 1.7286475408285996e-36, 1.7484861258538989e-37, 3.5210186699128533e-37),
+    (5, 5, 1.7426501600901373e-36, 4.7370142635342659e-36, 3.7248861049956034e-37, 1.0125290212289139e-36),
+    (5, 50, 1.6703173370166646e-36, 4.0871317668903464e-34, 8.4196498590303211e-37, 2.0602203929942999e-34),
+    (50, 2, 3.6039543137528758e-36, 6.5329687806960597e-34, 5.2266221327540312e-37, 9.4744151143860744e-35),
+    (50, 5, 7.222632008133751e-36, 1.7673197821036537e-33, 1.0588883354811727e-36, 2.5910143286093217e-34),
+    (50, 50, 3.7405176147900196e-36, 8.2390383297044382e-32, 7.995294986861833e-37, 1.7610809154750178e-32),
+]
+
+
+def test_pair_kernels_vs_reference_python_table(port):
+    """tests_pair/test_pair_kernels.cpp: the reference itself only prints the
+    % difference to an older Python code (constants have changed since), so
+    this pin is loose: agreement within 1 %."""
+    for w, wp, ee, ea, xe, xa in PAIR_PY:
+        o = port.pair_kernel(10., 84.181299999999993, w, wp) * 1e-21
+        got = np.array([o[0], o[4], o[2], o[6]])
+        assert np.max(rel_err(got, [ee, ea, xe, xa])) < 1e-2
+
+
+def _ccsn_profile():
+    path = os.path.join(REF_DIR, "inputs/nurates_CCSN/nurates_1.008E+01.txt")
+    if not os.path.exists(path):
+        pytest.skip("reference inputs not present on this host")
+    return np.loadtxt(path, comments="#"), 10.079454858851342
+
+
+@pytest.mark.parametrize("suffix,use_dU", [("", 0), ("_dU", 1)])
+def test_beta_regression_table(port, suffix, use_dU):
+    """tests_beta/test_beta_1.008e+01{,_dU}.txt columns 17-20 (the reference C
+    rates, printed to 7 digits).  The reference's loop covers zones
+    0..n_data-2 only (test_beta.cpp: RangePolicy(0, n_data - 1)), so the
+    last printed row is zeros and is left out."""
+    inp, omega = _ccsn_profile()
+    tab = np.loadtxt(os.path.join(REF_DIR, f"tests/tests_beta/test_beta_1.008e+01{suffix}.txt"),
+                     comments="#")
+    got = []
+    for r in inp:
+        eos = [r[2] / kBS_Mu * 1e-21, r[3], r[4], r[9], r[10], 0., r[6] + kBS_Q, r[5], 0.,
+               r[11], 0.]
+        o = port.abs_opacity(eos, [use_dU, 0, 1, 0, 0, 0, 0, 0], omega, 0)
+        got.append([o[1], o[0] / kBS_Clight * 1e7, o[3], o[2] / kBS_Clight * 1e7])
+    got = np.array(got)[:-1]
+    assert np.all(tab[-1, 16:20] == 0.)
+    assert np.max(rel_err(got, tab[:-1, 16:20], floor=1e-300)) < 1e-6
+
+
+def test_iso_regression_table(port):
+    """tests_iso/test_iso_1.008e+01.txt column 13 (reference C R_iso with WM)."""
+    inp, omega = _ccsn_profile()
+    tab = np.loadtxt(os.path.join(REF_DIR, "tests/tests_iso/test_iso_1.008e+01.txt"),
+                     comments="#")
+    got = []
+    for r in inp:
+        eos = [r[2] / kBS_Mu * 1e-21, r[3], 0., r[9], r[10], 0., 0., 0., 0., 0., 0.]
+        o = port.iso_scatt(eos, [0, 0, 0, 1, 0, 0, 0, 0], omega, 0)[0]
+        got.append(o * omega * omega * 4. * PI / kBS_Clight * 1e7)
+    assert np.max(rel_err(got, tab[:, 12])) < 1e-6
+
+
+def test_distribution_regression_table(port):
+    """tests_distribution/data: 102 M1 states and the reference's printed
+    distribution parameters.  The table predates a unit change of the energy
+    density: temperatures there are ours / kBS_MeV (and beta_f scales as
+    T^-(c_f+3)); every other column compares directly."""
+    d = os.path.join(REF_DIR, "tests/tests_distribution/data")
+    if not os.path.isdir(d):
+        pytest.skip("reference data not present on this host")
+    din = np.loadtxt(os.path.join(d, "distribution_function_m1_data.txt"), comments="#")
+    dout = np.loadtxt(os.path.join(d, "distribution_function_params_from_m1.txt"), comments="#")
+    m1 = np.zeros((12, din.shape[0]))
+    for s, c in ((0, 4), (1, 7), (2, 10), (3, 10)):
+        m1[s], m1[4 + s], m1[8 + s] = din[:, c], din[:, c + 1], din[:, c + 2]
+    dist = port.distr_from_m1(np.zeros((11, din.shape[0])), m1)
+    scale = [1., 1. / kBS_MeV, 1., 1., 1. / kBS_MeV, 1., kBS_MeV ** 3.6]
+    for s in range(3):
+        for q in range(7):
+            got = dist[4 * q + s] * scale[q]
+            assert np.max(rel_err(got, dout[:, 7 * s + q])) < 2e-6, (s, q)
+
+
+# --------------------------------------------------------------------------
+# 2. bit-for-bit against the reference build
+# --------------------------------------------------------------------------
+
+CASES = [
+    ([1, 1, 1, 0, 1], [1, 0, 1, 1, 1, 0, 1, 0], 10, 1),
+    ([1, 1, 1, 1, 1], [1, 0, 1, 1, 1, 0, 1, 0], 10, 1),
+    ([1, 1, 1, 1, 1], [1, 1, 1, 1, 1, 1, 0, 1], 10, 0),
+    ([1, 1, 1, 1, 1], [0, 0, 0, 0, 0, 2, 1, 0], 20, 1),
+    ([0, 0, 0, 1, 0], [1, 0, 1, 1, 1, 0, 1, 0], 7, 1),
+    ([1, 0, 0, 0, 1], [1, 0, 1, 1, 1, 0, 1, 0], 3, 1),
+]
+
+
+@pytest.mark.parametrize("flags,pars,nq,stim", CASES)
+def test_port_bitwise_vs_reference_grey(port, ref, flags, pars, nq, stim):
+    import bns_nurates_gb300 as bn
+    eos, m1 = bn.synthetic_points(7, 48, first=nq * 1000 + stim)
+    q = ref.gauss_legendre(nq)
+    a = port.m1_opacities(eos, m1, flags, pars, q, stim_abs=stim)
+    b = ref.m1_opacities(eos, m1, flags, pars, q, stim_abs=stim)
+    assert np.array_equal(a, b, equal_nan=True)
+
+
+def test_port_bitwise_vs_reference_spectral_and_distr(port, ref):
+    import bns_nurates_gb300 as bn
+    eos, m1 = bn.synthetic_points(8, 12)
+    q = ref.gauss_legendre(10)
+    e = np.logspace(0, np.log10(300.), 7)
+    for stim in (0, 1):
+        a = port.spectral(eos, m1, [1, 1, 1, 1, 1], [1, 0, 1, 1, 1, 2, 1, 0], q, e, stimulated=stim)
+        b = ref.spectral(eos, m1, [1, 1, 1, 1, 1], [1, 0, 1, 1, 1, 2, 1, 0], q, e, stimulated=stim)
+        assert np.array_equal(a, b, equal_nan=True)
+    assert np.array_equal(port.distr_from_m1(eos, m1), ref.distr_from_m1(eos, m1))
+    for u, v in zip(port.nu_equilibrium(eos), ref.nu_equilibrium(eos)):
+        assert np.array_equal(u, v)
+
+
+def test_port_bitwise_vs_reference_fdi(port, ref):
+    x = np.concatenate([np.linspace(-80., 80., 4001), [-2., 0., 2., np.nan]])
+    for k in range(6):
+        assert np.array_equal(port.fdi(k, x), ref.fdi(k, x), equal_nan=True)
+
+
+# --------------------------------------------------------------------------
+# 3. against the golden fixtures (work on any host)
+# --------------------------------------------------------------------------
+
+GREY_FIXTURES = ["grey_hr98_n10.npz", "grey_all_hr98_n10.npz", "grey_all_gp19_n20.npz",
+                 "grey_brt06_nostim.npz", "grey_given_distr.npz"]
+
+
+@pytest.mark.parametrize("name", GREY_FIXTURES)
+def test_port_vs_golden_grey(port, name):
+    g = golden(name)
+    distr = g["distr"] if g["distr"].size else None
+    out = port.m1_opacities(g["eos"], g["m1"], g["flags"], g["pars"], (g["x"], g["w"]),
+                            distr=distr, stim_abs=int(g["stim"]))
+    assert np.max(rel_err(out, g["out"], floor=1e-300)) < 1e-13
+
+
+def test_port_vs_golden_spectral(port):
+    g = golden("spectral_n10.npz")
+    for stim in (0, 1):
+        out = port.spectral(g["eos"], g["m1"], g["flags"], g["pars"], (g["x"], g["w"]),
+                            g["energies"], stimulated=stim)
+        assert np.max(rel_err(out, g[f"stim{stim}"], floor=1e-300)) < 1e-13
+
+
+def test_port_vs_golden_point_a(port):
+    g = golden("point_a.npz")
+    out = port.m1_opacities(g["eos"], g["m1"], [1, 1, 1, 1, 1], g["pars"], (g["x"], g["w"]))
+    assert np.max(rel_err(out, g["out"], floor=1e-300)) < 1e-13
+
+
+def test_layout_fixture_present():
+    with open(os.path.join(GOLDEN, "layout.json")) as f:
+        lay = json.load(f)
+    assert lay["MyQuadrature"]["__size__"] == 400
+    assert lay["GreyOpacityParams"]["__size__"] > 0
