@@ -1,0 +1,101 @@
+// Single-precision device physics of the mixed-precision path.
+//
+// Only bounded, cancellation-free shape functions run in FP32; their
+// dimensionful prefactors, every Fermi-Dirac integral and the distribution
+// algebra stay in FP64 (bnsn_fp64.cuh).
+#pragma once
+
+#include <math.h>
+
+#include "bnsn_constants.h"
+#include "bnsn_fp64.cuh"
+
+namespace bnsn {
+namespace fp32 {
+
+#define BNSN_DI __device__ __forceinline__
+
+// HR98 bremsstrahlung (kernel_brem_HR98.hpp:33-338) split into per-point FP64
+// constants (below, rounded to FP32) and an FP32 shape of x = (w + w')/T:
+//   s_abs(x) = outer * sum_ch pre_ch * S_ch(x) / (x^2 + hgg_ch^2)
+// with outer = 3 C_brem / medium correction and pre_ch = n_ch gamma_ch / T.
+struct Hr98Mixed
+{
+    float y, ey12, poly_y, y4p1, Dy, p, pinv;
+    float K1[3], f_u[3], eta2p1[3], sqe[3], ep2[3], h[3], hgg2[3], pre[3];
+    double outer;
+};
+
+BNSN_DI void hr98_mixed_from(const fp64::Hr98Point& P, Hr98Mixed* M)
+{
+    M->y      = (float)P.y;
+    M->ey12   = (float)P.ey12;
+    M->poly_y = (float)P.poly_y;
+    M->y4p1   = (float)P.y4p1;
+    M->Dy     = (float)P.Dy;
+    M->p      = (float)(-P.mp);
+    M->pinv   = (float)(-P.minv);
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+    {
+        const fp64::Hr98Channel& C = P.ch[c];
+        M->K1[c]     = (float)C.K1;
+        M->f_u[c]    = (float)C.f_u;
+        M->eta2p1[c] = (float)C.eta2p1;
+        M->sqe[c]    = (float)C.sqe;
+        M->ep2[c]    = (float)C.ep2;
+        M->h[c]      = (float)C.h;
+        M->hgg2[c]   = (float)(C.hgg * C.hgg);
+        M->pre[c]    = (float)(C.weight * C.gamma / P.T);
+    }
+    M->outer = 3. * k::BremConst / P.mcorr;
+}
+
+// Sum over the three NN channels of n gamma S(x) / (T (x^2 + (gamma g/2)^2)).
+// The interpolation (s_nd^-p + s_d^-p)^(-1/p) of Eq.(49) is evaluated as
+// min * (1 + (max/min)^-p)^(-1/p): the same value, but the outer power acts on
+// a number in [1, 2], which keeps its FP32 rounding error at the ulp level
+// instead of growing with |p log s|.
+BNSN_DI float hr98_shape(const Hr98Mixed& M, float x_in)
+{
+    const float x   = fmaxf(x_in, (float)k::BremXmin);
+    const float y   = M.y;
+    const float X   = x + 2.f - M.ey12;
+    const float q   = (float)k::Pi18 + x + y;
+    const float snd = 2.f * (float)k::SqrtPi * (X * sqrtf(X)) * (x * x + 2.f * x * y + M.poly_y + 1.f) /
+                      ((float)k::SqrtPi + (q * q) * (q * q));
+    const float em1 = -expm1f(-x);
+    const float X2  = x * x + (float)k::FourPiSq;
+    const float lx  = logf(x);
+    const float px11  = expf(1.1f * lx);
+    const float px093 = expf(0.93f * lx);
+    const float px12  = expf(1.2f * lx);
+    const float px28  = expf(2.8f * lx);
+    const float x2    = x * x;
+    const float xterm = 3.f + (x - 1.2f) * (x - 1.2f) + 1.f / (x2 * x2);
+    const float gpart = 0.0044f * px11 * y / M.Dy;
+    const float cden2 = 30.f + 0.005f * px28;
+    const float xs2   = x_in * x_in;
+    float tot         = 0.f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+    {
+        const float s_d    = M.K1[c] * X2 * x * M.f_u[c] / ((float)k::FourPiSq * em1);
+        const float lo     = fminf(snd, s_d);
+        const float hi     = fmaxf(snd, s_d);
+        const float t      = expf(-M.p * logf(hi / lo));
+        const float s_base = lo * expf(-log1pf(t) * M.pinv);
+        const float f_brem = 1.f + 1.f / (xterm * M.eta2p1[c] * M.y4p1);
+        const float g_brem = 1.f - gpart * M.sqe[c] / M.ep2[c];
+        const float c_brem =
+            1.1f * px11 * M.h[c] / (2.3f + M.h[c] * px093 + 0.0001f * px12) * 30.f / cden2;
+        const float s = s_base * f_brem * (1.f + c_brem * g_brem);
+        tot += M.pre[c] * s / (xs2 + M.hgg2[c]);
+    }
+    return tot;
+}
+
+#undef BNSN_DI
+
+} // namespace fp32
+} // namespace bnsn

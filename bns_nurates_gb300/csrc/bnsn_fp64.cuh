@@ -571,51 +571,61 @@ struct PairEnergyFdi
     double m[5], p[5];
 };
 
-// Kernel at (omega = y T, omega' = z T): em[4], ab[4].  fa / fb hold the
-// per-energy Fermi integrals of y and z; f3e / f4e are F_3(eta), F_4(eta).
+// Psi_0(y, z) and Psi_0(z, y) of kernel_pair.hpp:16-120 from the per-energy
+// Fermi integrals: fam[k-1] = F_k(eta - y), fap = F_k(eta + y), fbm / fbp the
+// same for z; f3e / f4e are F_3(eta), F_4(eta).  Zero when eta - y - z > 200.
+BNSN_DI void pair_psi(double eta, double y, double z, const double* fam, const double* fap,
+                      const double* fbm, const double* fbp, double f3e, double f4e,
+                      double* psi0, double* psi1)
+{
+    *psi0 = 0.;
+    *psi1 = 0.;
+    if (eta - y - z > 200.)
+        return;
+    double fmyz[3], fpyz[3];
+    fdi_orders<3, 5>(eta - y - z, fmyz);
+    fdi_orders<3, 5>(eta + y + z, fpyz);
+    const double c0  = 20. * fam[3];
+    const double c1  = 20. * fbp[3];
+    const double c2  = 120. * fam[1] - 120. * fbp[1];
+    const double c3  = -40. * fam[2] + 40. * fbp[2];
+    const double c4  = 40. * f3e;
+    const double c5  = 40. * fmyz[0] - c4;
+    const double c6  = -20. * f4e;
+    const double c7  = 20. * fmyz[1] + c6;
+    const double c8  = -40. * fpyz[0] + c4;
+    const double c9  = 20. * fpyz[1] + c6;
+    const double c10 = -4. * fam[4] + 4. * fmyz[2] - 4. * fbm[4] + 4. * fap[4] -
+                       4. * fpyz[2] + 4. * fbp[4];
+    const double c11 = 20. * fap[3];
+    const double c12 = 20. * fbm[3];
+    const double c13 = -40. * fbm[2] + 40. * fap[2];
+    const double c14 = 120. * fbm[1] - 120. * fap[1];
+    const double yz  = y * z;
+    const double den = 15. * (yz * yz);
+    const double p0 =
+        c10 +
+        y * (-c0 + c1 + c7 +
+             y * (c3 + c5 + z * (c2 + z * (-120. * fam[0] + 120. * fbp[0]))) +
+             z * (80. * fam[2] - 80. * fbp[2] - c2 * z)) +
+        z * (c0 - c1 + c9 + z * (c3 + c8));
+    const double p1 =
+        c10 + y * (-c11 + c12 + c9 + y * (c13 + c8)) +
+        z * (c11 - c12 + c7 + y * (80. * fbm[2] - 80. * fap[2] - c14 * y) +
+             z * (c13 + c5 + y * (c14 + y * (-120. * fbm[0] + 120. * fap[0]))));
+    *psi0 = p0 / den;
+    *psi1 = p1 / den;
+}
+
+// Pair kernel at (omega = y T, omega' = z T), kernel_pair.hpp:135-198:
+// em[4] = Phi/2 per species, ab[4] = e^{(w + w')/T} em.
 BNSN_DI void pair_kernel(double T, double eta, double omega, double omega_p,
                          double y, double z, const double* fam, const double* fap,
                          const double* fbm, const double* fbp, double f3e,
                          double f4e, double* em, double* ab)
 {
-    double psi0 = 0., psi1 = 0.;
-    if (!(eta - y - z > 200.))
-    {
-        double fmyz[3], fpyz[3];
-        fdi_orders<3, 5>(eta - y - z, fmyz);
-        fdi_orders<3, 5>(eta + y + z, fpyz);
-        // fam[k-1] = F_k(eta - y), fap = F_k(eta + y), fbm / fbp for z
-        const double c0  = 20. * fam[3];
-        const double c1  = 20. * fbp[3];
-        const double c2  = 120. * fam[1] - 120. * fbp[1];
-        const double c3  = -40. * fam[2] + 40. * fbp[2];
-        const double c4  = 40. * f3e;
-        const double c5  = 40. * fmyz[0] - c4;
-        const double c6  = -20. * f4e;
-        const double c7  = 20. * fmyz[1] + c6;
-        const double c8  = -40. * fpyz[0] + c4;
-        const double c9  = 20. * fpyz[1] + c6;
-        const double c10 = -4. * fam[4] + 4. * fmyz[2] - 4. * fbm[4] + 4. * fap[4] -
-                           4. * fpyz[2] + 4. * fbp[4];
-        const double c11 = 20. * fap[3];
-        const double c12 = 20. * fbm[3];
-        const double c13 = -40. * fbm[2] + 40. * fap[2];
-        const double c14 = 120. * fbm[1] - 120. * fap[1];
-        const double yz  = y * z;
-        const double den = 15. * (yz * yz);
-        const double p0 =
-            c10 +
-            y * (-c0 + c1 + c7 +
-                 y * (c3 + c5 + z * (c2 + z * (-120. * fam[0] + 120. * fbp[0]))) +
-                 z * (80. * fam[2] - 80. * fbp[2] - c2 * z)) +
-            z * (c0 - c1 + c9 + z * (c3 + c8));
-        const double p1 =
-            c10 + y * (-c11 + c12 + c9 + y * (c13 + c8)) +
-            z * (c11 - c12 + c7 + y * (80. * fbm[2] - 80. * fap[2] - c14 * y) +
-                 z * (c13 + c5 + y * (c14 + y * (-120. * fbm[0] + 120. * fap[0]))));
-        psi0 = p0 / den;
-        psi1 = p1 / den;
-    }
+    double psi0, psi1;
+    pair_psi(eta, y, z, fam, fap, fbm, fbp, f3e, f4e, &psi0, &psi1);
     const double aux = k::PairPhi * (T * T) / (1. - safe_exp(y + z));
     const double phi0 = ((k::PairA1e * k::PairA1e) * psi0 + (k::PairA2e * k::PairA2e) * psi1) * aux;
     const double phi1 = ((k::PairA1e * k::PairA1e) * psi1 + (k::PairA2e * k::PairA2e) * psi0) * aux;
@@ -629,6 +639,33 @@ BNSN_DI void pair_kernel(double T, double eta, double omega, double omega_p,
 #pragma unroll
     for (int s = 0; s < 4; ++s)
         ab[s] = ex * em[s];
+}
+
+// The same kernel with one exponential: with D = 1 - e^{-s}, s = y + z,
+// 1/(1 - e^s) = -e^{-s}/D and e^s/(1 - e^s) = -1/D, so
+// em = -(Phi T^2/2) A e^{-s}/D and ab = -(Phi T^2/2) A / D; stable for any s
+// (the reference's clamped e^{+s} never appears).  Used by the mixed path.
+BNSN_DI void pair_kernel_one_exp(double T, double eta, double y, double z, const double* fam,
+                                 const double* fap, const double* fbm, const double* fbp,
+                                 double f3e, double f4e, double* em, double* ab)
+{
+    double psi0, psi1;
+    pair_psi(eta, y, z, fam, fap, fbm, fbp, f3e, f4e, &psi0, &psi1);
+    const double s   = y + z;
+    const double D   = -expm1(-s);
+    const double K   = -0.5 * k::PairPhi * (T * T) / D;
+    const double ems = 1. - D; // e^{-s}
+    const double a0  = (k::PairA1e * k::PairA1e) * psi0 + (k::PairA2e * k::PairA2e) * psi1;
+    const double a1  = (k::PairA1e * k::PairA1e) * psi1 + (k::PairA2e * k::PairA2e) * psi0;
+    const double a2  = (k::PairA1x * k::PairA1x) * psi0 + (k::PairA2x * k::PairA2x) * psi1;
+    const double a3  = (k::PairA1x * k::PairA1x) * psi1 + (k::PairA2x * k::PairA2x) * psi0;
+    ab[0] = K * a0;
+    ab[1] = K * a1;
+    ab[2] = K * a2;
+    ab[3] = K * a3;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        em[q] = ab[q] * ems;
 }
 
 // ---------------------------------------------------------------------------

@@ -30,6 +30,7 @@ struct OpacityLaunch
     int use_dU, use_dm_eff, use_WM_ab, use_WM_sc, use_decay, brem_impl;
     int use_medium, neglect_blocking;
     int stim;
+    int mixed;             // 0: all FP64, 1: mixed precision
     double gamma36;        // GammaStirling(3.6), host libm
     int n1, n2, ncell;
     double x1[kMaxQ], w1[kMaxQ], x2[kMaxQ], w2[kMaxQ];
@@ -47,7 +48,11 @@ struct OpacityLaunch
     double* sout[16];      // j, kappa, j_s, kappa_s per species
 };
 
-cudaError_t launch_grey_fp64(const OpacityLaunch& L, cudaStream_t stream, int num_sms);
+// Grey opacities in chunks of ws_points points; ws holds ws_points per-point
+// scratch records of grey_point_scratch_bytes() each.
+size_t grey_point_scratch_bytes();
+cudaError_t launch_grey(const OpacityLaunch& L, cudaStream_t stream, int num_sms, double* ws,
+                        int64_t ws_points);
 cudaError_t launch_spectral_fp64(const OpacityLaunch& L, cudaStream_t stream, int num_sms);
 struct DistrLaunch
 {

@@ -2,9 +2,14 @@
 //
 // This layer validates arguments, turns the reference structs
 // (MyQuadrature, OpacityFlags, OpacityParams) into a by-value launch
-// descriptor and launches on the caller's stream.  The batched calls never
-// allocate; the per-point drop-ins and the host-buffer batch stage through a
-// per-device buffer allocated on first use.
+// descriptor and launches on the caller's stream.
+//
+// Device memory: the grey call takes its per-point scratch records (at most
+// kGreyChunk points at a time) from a library-owned stream-ordered memory
+// pool, allocated and freed in order on the caller's stream, so calls on
+// different streams never share scratch.  The pool keeps its memory after the
+// first call.  The per-point drop-ins and the host-buffer batch stage their
+// inputs through a per-device buffer allocated on first use.
 
 #include <cuda_runtime.h>
 #include <math.h>
@@ -47,7 +52,12 @@ struct DeviceState
     void* stage  = nullptr; // staging area of the host-buffer APIs
     size_t stage_bytes = 0;
     cudaStream_t streams[2] = {nullptr, nullptr};
+    cudaMemPool_t pool = nullptr; // grey scratch records
 };
+
+// Points per grey scratch chunk: 16384 records of ~6 KB stay resident in L2
+// between the phase kernels of a chunk.
+constexpr int64_t kGreyChunk = 16384;
 
 std::mutex g_mu;
 std::map<int, DeviceState> g_dev;
@@ -72,6 +82,22 @@ int device_state(DeviceState** out)
         if ((e = cudaDeviceGetAttribute(&st.num_sms, cudaDevAttrMultiProcessorCount, dev)) !=
             cudaSuccess)
             return cuda_fail(e, "cudaDeviceGetAttribute");
+        cudaMemPoolProps props = {};
+        props.allocType     = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id   = dev;
+        if ((e = cudaMemPoolCreate(&st.pool, &props)) != cudaSuccess)
+        {
+            st.num_sms = 0;
+            return cuda_fail(e, "cudaMemPoolCreate");
+        }
+        uint64_t keep = UINT64_MAX;
+        if ((e = cudaMemPoolSetAttribute(st.pool, cudaMemPoolAttrReleaseThreshold, &keep)) !=
+            cudaSuccess)
+        {
+            st.num_sms = 0;
+            return cuda_fail(e, "cudaMemPoolSetAttribute");
+        }
     }
     *out = &st;
     return BNSN_OK;
@@ -280,11 +306,23 @@ int bnsn_m1_opacities(const MyQuadrature* quad_1d, const MyQuadrature* quad_2d,
                 return fail(BNSN_ERR_ARG, "an output pointer is NULL");
             L.out[q * 4 + s] = o[q][s];
         }
+    L.mixed = precision == BNSN_MIXED;
     DeviceState* st;
     if ((rc = attach_device(&L, &st)))
         return rc;
-    cudaError_t e = launch_grey_fp64(L, (cudaStream_t)stream, st->num_sms);
-    return e == cudaSuccess ? BNSN_OK : cuda_fail(e, "grey kernel launch");
+    if (npts == 0)
+        return BNSN_OK;
+    const int64_t ws_points = std::min<int64_t>(npts, kGreyChunk);
+    double* ws = nullptr;
+    cudaError_t e = cudaMallocFromPoolAsync((void**)&ws, ws_points * grey_point_scratch_bytes(),
+                                           st->pool, (cudaStream_t)stream);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "grey scratch allocation");
+    e = launch_grey(L, (cudaStream_t)stream, st->num_sms, ws, ws_points);
+    const cudaError_t ef = cudaFreeAsync(ws, (cudaStream_t)stream);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "grey kernel launch");
+    return ef == cudaSuccess ? BNSN_OK : cuda_fail(ef, "grey scratch release");
 }
 
 int bnsn_spectral_opacities(const MyQuadrature* quad_1d, const OpacityFlags* flags,

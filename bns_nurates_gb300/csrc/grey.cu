@@ -1,0 +1,837 @@
+// Grey M1 opacity kernels (sm_103a), FP64 and mixed precision.
+//
+// Restates ComputeM1OpacitiesGenericFormalism (m1_opacities.hpp:1062-1295)
+// with the integration rules of integration.hpp:608-844, as five phase
+// kernels over a chunk of points.  Each phase has a small hot loop shared by
+// all resident warps, so the instruction working set stays in the SM's
+// instruction cache (a single fused kernel spent most of its issue slots
+// waiting on instruction fetch):
+//
+//   prelude : per point (one warp): distribution parameters, Fermi integrals
+//             at +-eta_e, brem channel constants, the 2n-energy tables of the
+//             double integral (distribution values, F_k(eta +- w/T)), and the
+//             1-D beta and iso-scattering integrals; the per-point record is
+//             staged in shared memory and written to the scratch arena.
+//   pair    : per point (one warp): the M(M+1)/2 unordered (w, w') cells of
+//             the pair kernel, one evaluation filling (w, w') and (w', w),
+//             weighted and summed into the number and energy moments.
+//   brem    : the same cells for the bremsstrahlung kernel (HR98, BRT06, GP19).
+//   neps    : per point (one warp): the 2 n^2 (nu, nubar) pairs of the NES/NPS
+//             double integral, both directions from one set of Fermi integrals.
+//   final   : per point (one thread): assembly of the 20 outputs.
+//
+// The reference's 2n x 2n integrand matrices (m1_opacities.hpp:774-1057) are
+// never materialised: every cell is multiplied by its quadrature weight and
+// summed directly; lane sums are combined with warp shuffles.
+//
+// MIXED = false: every operation in FP64 (the plain path).
+// MIXED = true : the HR98 bremsstrahlung shape of each cell runs in FP32
+// (bnsn_fp32.cuh) and the pair kernel takes one expm1 instead of two
+// exponentials; Fermi-Dirac integrals, the pair Psi polynomial (catastrophic
+// cancellation), distribution reconstruction, detailed balance and the
+// distribution-weighted sums stay FP64.
+
+#include <cuda_runtime.h>
+
+#include "bnsn_fp32.cuh"
+#include "bnsn_fp64.cuh"
+#include "bnsn_internal.h"
+
+namespace bnsn {
+
+using namespace fp64;
+
+// Per-point record in the scratch arena (double words only, no padding).
+struct PointTab
+{
+    Distr d;
+    double fe[2][6];  // F_0..F_5 at eta_e and -eta_e
+    double fd0[2];    // FermiDistr(0, 1, +-eta_e)
+    Hr98Point hr;
+    double brt06_pre;
+    double eta_pp, eta_nn;
+    double same_cf;
+    double nu[kMaxM];    // energies of the double-integral grid
+    double y[kMaxM];     // nu / T
+    double g[kMaxM][4];  // TotalNuF at nu per species
+    double fm[kMaxM][5]; // F_1..F_5 at eta_e - nu/T
+    double fp[kMaxM][5]; // F_1..F_5 at eta_e + nu/T
+    double s2d[16];      // pair + brem: n-moment em/ab, J-moment em/ab
+    double snes[16];     // NES/NPS, same layout
+    double sbeta[8];     // beta: n_em[2], j_em[2], n_ab[2], j_ab[2]
+    double siso[4];      // iso per species
+};
+static_assert(sizeof(PointTab) % sizeof(double) == 0, "PointTab must be double words");
+constexpr int kTabWords = sizeof(PointTab) / sizeof(double);
+
+size_t grey_point_scratch_bytes() { return sizeof(PointTab); }
+
+namespace {
+
+constexpr int kWarps = 4; // warps per CTA in the per-point kernels
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ double total_nu_f1(double omega, const Distr& d, int s)
+{
+    const double ft = fermi_distr(omega, d.temp_t[s], d.temp_t[s] * d.eta_t[s]);
+    const double fn = d.beta_f[s] * pow(omega, d.c_f[s]) * exp(-omega / d.temp_f[s]);
+    return d.w_t[s] * ft + d.w_f[s] * fn;
+}
+
+// Cooperative copy of `words` doubles (lane-strided, coalesced).
+__device__ __forceinline__ void warp_copy(double* __restrict__ dst,
+                                          const double* __restrict__ src, int words,
+                                          int lane)
+{
+    for (int k = lane; k < words; k += 32)
+        dst[k] = src[k];
+}
+
+// s_beta of m1_opacities.hpp:1093-1110 from F_4, F_5 at +-eta_e.
+__device__ __forceinline__ void beta_scales(double T, double eta_e, const double (&fe)[2][6],
+                                            double* sb)
+{
+    if (eta_e > -30. && eta_e < 30.)
+    {
+        sb[0] = T * fe[0][5] / fe[0][4];
+        sb[1] = T * fe[1][5] / fe[1][4];
+    }
+    else if (eta_e > 30.)
+    {
+        sb[0] = T * eta_e * 0.8333333333333333;
+        sb[1] = T * 5.;
+    }
+    else
+    {
+        sb[0] = T * 5.;
+        sb[1] = T * eta_e * 0.8333333333333333;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// prelude
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kWarps * 32)
+    grey_prelude_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
+                        double* __restrict__ scratch)
+{
+    __shared__ double s_B1[kMaxM], s_x1[kMaxQ], s_x2[kMaxQ];
+    __shared__ PointTab s_tab[kWarps];
+    for (int k = threadIdx.x; k < kMaxM; k += blockDim.x)
+        s_B1[k] = L.B1[k];
+    for (int k = threadIdx.x; k < kMaxQ; k += blockDim.x)
+    {
+        s_x1[k] = L.x1[k];
+        s_x2[k] = L.x2[k];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    PointTab& W    = s_tab[threadIdx.x >> 5];
+    const int n1 = L.n1, n2 = L.n2, M = 2 * n2;
+    const int64_t nwarp = (int64_t)gridDim.x * kWarps;
+
+    for (int64_t q = (int64_t)blockIdx.x * kWarps + (threadIdx.x >> 5); q < np; q += nwarp)
+    {
+        const int64_t p = p0 + q;
+        const double nb = L.eos[0][p], T = L.eos[1][p];
+        const double yp = L.eos[3][p], yn = L.eos[4][p];
+        const double mu_e = L.eos[7][p];
+        const double eta_e = mu_e / T;
+
+        if (L.has_distr)
+        {
+            if (lane < 28)
+                (&W.d.w_t[0])[lane] = L.distr[lane][p];
+        }
+        else if (lane < 4)
+        {
+            const int s = lane;
+            distr_species(L.m1[s][p], L.m1[4 + s][p], L.m1[8 + s][p], L.gamma36, &W.d.w_t[s],
+                          &W.d.temp_t[s], &W.d.eta_t[s], &W.d.w_f[s], &W.d.temp_f[s],
+                          &W.d.c_f[s], &W.d.beta_f[s]);
+        }
+        if (lane == 4 || lane == 5)
+        {
+            const int e     = lane - 4;
+            const double et = e ? -mu_e / T : eta_e;
+            fdi_orders<0, 5>(et, W.fe[e]);
+            W.fd0[e] = fermi_distr(0., 1., et);
+        }
+        if (L.use_brem && L.brem_impl == 0)
+        {
+            if (lane >= 6 && lane < 9)
+                W.hr.ch[lane - 6] = hr98_channel(nb, yn, yp, T, lane - 6);
+            if (lane == 9)
+                hr98_point_common(nb, T, L.use_medium != 0, &W.hr);
+        }
+        if (lane == 10 && L.use_brem && L.brem_impl == 1)
+            W.brt06_pre = brt06_point(nb, T, yn, yp);
+        if (lane == 11 && L.use_iso)
+        {
+            W.eta_pp = eta_nn_sc(nb, T, yp);
+            W.eta_nn = eta_nn_sc(nb, T, yn);
+        }
+        __syncwarp();
+        if (lane == 0)
+        {
+            const double c0 = W.d.c_f[0];
+            W.same_cf = ((W.d.c_f[1] == c0) && (W.d.c_f[2] == c0) && (W.d.c_f[3] == c0)) ? 1. : 0.;
+        }
+        __syncwarp();
+        const bool same_cf = W.same_cf != 0.;
+
+        // energy tables of the double integral (m1_opacities.hpp:783-787)
+        if (L.use_pair || L.use_brem)
+        {
+            const double t2d = k::TempMultiple * T;
+            for (int a = lane; a < M; a += 32)
+            {
+                const int i     = a < n2 ? a : a - n2;
+                const double nu = a < n2 ? t2d * s_x2[i] : t2d / s_x2[i];
+                W.nu[a]         = nu;
+                W.y[a]          = nu / T;
+                total_nu_f4(nu, W.d, same_cf, W.g[a]);
+            }
+            if (L.use_pair)
+            {
+                for (int qq = lane; qq < 2 * M; qq += 32)
+                {
+                    const int a     = qq >> 1;
+                    const int i     = a < n2 ? a : a - n2;
+                    const double nu = a < n2 ? t2d * s_x2[i] : t2d / s_x2[i];
+                    const double y  = nu / T;
+                    if (qq & 1)
+                        fdi_orders<1, 5>(eta_e + y, W.fp[a]);
+                    else
+                        fdi_orders<1, 5>(eta_e - y, W.fm[a]);
+                }
+            }
+        }
+
+        // beta processes (m1_opacities.hpp:93-237, integration.hpp:805-844)
+        if (L.use_abs_em)
+        {
+            double sb[2];
+            beta_scales(T, eta_e, W.fe, sb);
+            const BetaPoint bp =
+                beta_point(nb, T, yp, yn, L.eos[5][p], L.eos[6][p], mu_e, L.eos[9][p],
+                           L.eos[10][p], L.use_dU, L.use_dm_eff, L.use_WM_ab, L.use_decay);
+            double acc[8];
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk)
+                acc[kk] = 0.;
+            const int m1n = 2 * n1;
+            for (int it = lane; it < 2 * m1n; it += 32)
+            {
+                const int s = it >= m1n;
+                const int a = it - s * m1n;
+                const int i = a < n1 ? a : a - n1;
+                const double t  = sb[s];
+                const double nu = a < n1 ? t * s_x1[i] : t / s_x1[i];
+                const double g  = total_nu_f1(nu, W.d, s);
+                double ab, em;
+                beta_rates(bp, nu, s, &ab, &em);
+                if (L.stim)
+                    ab = ab + em;
+                const double nu2 = nu * nu;
+                const double ev  = nu2 * em;
+                const double av  = nu2 * g * ab;
+                const double wn  = s_B1[a];
+                const double wj  = wn * nu;
+                if (s == 0)
+                {
+                    acc[0] += wn * ev;
+                    acc[2] += wj * ev;
+                    acc[4] += wn * av;
+                    acc[6] += wj * av;
+                }
+                else
+                {
+                    acc[1] += wn * ev;
+                    acc[3] += wj * ev;
+                    acc[5] += wn * av;
+                    acc[7] += wj * av;
+                }
+            }
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk)
+                acc[kk] = warp_sum(acc[kk]);
+            if (lane == 0)
+            {
+#pragma unroll
+                for (int kk = 0; kk < 8; ++kk)
+                    W.sbeta[kk] = acc[kk];
+            }
+        }
+
+        // iso-energetic scattering (m1_opacities.hpp:39-91, integration.hpp:770-802)
+        if (L.use_iso)
+        {
+            double s_iso[4];
+#pragma unroll
+            for (int s = 0; s < 4; ++s)
+            {
+                const double ns = L.m1[s][p];
+                s_iso[s] = (ns > k::ThresholdN) ? (L.m1[4 + s][p] / ns) : 1.5 * T;
+            }
+            double acc[4] = {0., 0., 0., 0.};
+            const int m1n = 2 * n1;
+            for (int it = lane; it < 4 * m1n; it += 32)
+            {
+                const int s = it / m1n;
+                const int a = it - s * m1n;
+                const int i = a < n1 ? a : a - n1;
+                const double t   = s == 0 ? s_iso[0] : s == 1 ? s_iso[1] : s == 2 ? s_iso[2] : s_iso[3];
+                const double nu  = a < n1 ? t * s_x1[i] : t / s_x1[i];
+                const double g   = total_nu_f1(nu, W.d, s);
+                const double iso = iso_scatt_total(nu, W.eta_pp, W.eta_nn, L.use_WM_sc != 0);
+                const double aux = 4. * k::Pi * (nu * nu) * (nu * nu) * nu * iso;
+                const double v   = g * aux * s_B1[a];
+                if (s == 0) acc[0] += v;
+                else if (s == 1) acc[1] += v;
+                else if (s == 2) acc[2] += v;
+                else acc[3] += v;
+            }
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+                acc[kk] = warp_sum(acc[kk]);
+            if (lane == 0)
+            {
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk)
+                    W.siso[kk] = acc[kk];
+            }
+        }
+        __syncwarp();
+        warp_copy(scratch + q * kTabWords, (const double*)&W, kTabWords, lane);
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// weight algebra of m1_opacities.hpp:577-758 for one directed cell (a, b):
+// em_s = K_em[s] bf_b[partner(s)], ab_s = K_ab[s] g_b[partner(s)], then
+// stimulated absorption and the nu^2 nubar^2 weight, summed with the number
+// (W1) and energy (W2) quadrature weights.  The moments are linear in the
+// kernel, so pair and brem contributions are summed in separate phases.
+// ---------------------------------------------------------------------------
+template <bool STIM>
+__device__ __forceinline__ void add_cell(double* acc, const double* Kem, const double* Kab,
+                                         const double* ga, const double* gb, bool nb_block,
+                                         double w4, double W1, double W2)
+{
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+    {
+        const int ps    = s ^ 1;
+        const double em = Kem[s] * (nb_block ? 1. : 1. - gb[ps]);
+        const double am = Kab[s] * gb[ps];
+        double EM, AB;
+        if (STIM)
+        {
+            AB = w4 * ga[s] * (em + am);
+            EM = em * w4;
+        }
+        else
+        {
+            AB = am * (w4 * ga[s]);
+            EM = em * (w4 * (1. - ga[s]));
+        }
+        acc[s] += EM * W1;
+        acc[4 + s] += AB * W1;
+        acc[8 + s] += EM * W2;
+        acc[12 + s] += AB * W2;
+    }
+}
+
+// Shared-memory copy of the energy tables a cell loop needs.
+struct CellTab
+{
+    double nu[kMaxM];
+    double y[kMaxM];
+    double g[kMaxM][4];
+    double fm[kMaxM][5];
+    double fp[kMaxM][5];
+    double f3e, f4e;
+    double brt06_pre;
+    Hr98Point hr;
+    fp32::Hr98Mixed hm;
+};
+
+__device__ __forceinline__ void load_cell_tab(CellTab& C, const PointTab* __restrict__ P,
+                                              int M, bool pair_tables, int lane)
+{
+    warp_copy(C.nu, P->nu, M, lane);
+    warp_copy(C.y, P->y, M, lane);
+    warp_copy(&C.g[0][0], &P->g[0][0], 4 * M, lane);
+    if (pair_tables)
+    {
+        warp_copy(&C.fm[0][0], &P->fm[0][0], 5 * M, lane);
+        warp_copy(&C.fp[0][0], &P->fp[0][0], 5 * M, lane);
+    }
+    if (lane == 0)
+    {
+        C.f3e       = P->fe[0][3];
+        C.f4e       = P->fe[0][4];
+        C.brt06_pre = P->brt06_pre;
+    }
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(kWarps * 32)
+    grey_pair_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
+                     double* __restrict__ scratch)
+{
+    __shared__ double s_A1[kMaxM], s_A2[kMaxM];
+    __shared__ uint32_t s_cells[kMaxCells];
+    __shared__ CellTab s_ct[kWarps];
+    for (int k = threadIdx.x; k < kMaxM; k += blockDim.x)
+    {
+        s_A1[k] = L.A1[k];
+        s_A2[k] = L.A2[k];
+    }
+    for (int k = threadIdx.x; k < L.ncell; k += blockDim.x)
+        s_cells[k] = L.cells[k];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    CellTab& C     = s_ct[threadIdx.x >> 5];
+    const int M    = 2 * L.n2;
+    const bool nbb = L.neglect_blocking != 0;
+    const int64_t nwarp = (int64_t)gridDim.x * kWarps;
+
+    for (int64_t q = (int64_t)blockIdx.x * kWarps + (threadIdx.x >> 5); q < np; q += nwarp)
+    {
+        const int64_t p  = p0 + q;
+        PointTab* P      = (PointTab*)(scratch + q * kTabWords);
+        const double T   = L.eos[1][p];
+        const double eta = L.eos[7][p] / T;
+        __syncwarp();
+        load_cell_tab(C, P, M, true, lane);
+        __syncwarp();
+        double acc[16];
+#pragma unroll
+        for (int kk = 0; kk < 16; ++kk)
+            acc[kk] = 0.;
+        for (int c = lane; c < L.ncell; c += 32)
+        {
+            const uint32_t ab = s_cells[c];
+            const int a = ab & 0xffffu, b = ab >> 16;
+            const double nua = C.nu[a], nub = C.nu[b];
+            double pe[4], pa[4];
+            if (MIXED)
+                pair_kernel_one_exp(T, eta, C.y[a], C.y[b], C.fm[a], C.fp[a], C.fm[b], C.fp[b],
+                                    C.f3e, C.f4e, pe, pa);
+            else
+                pair_kernel(T, eta, nua, nub, C.y[a], C.y[b], C.fm[a], C.fp[a], C.fm[b],
+                            C.fp[b], C.f3e, C.f4e, pe, pa);
+            const double w4 = (nua * nua) * (nub * nub);
+            const double W1 = s_A1[a] * s_A1[b];
+            if (L.stim)
+                add_cell<true>(acc, pe, pa, C.g[a], C.g[b], nbb, w4, W1, s_A2[a] * s_A1[b]);
+            else
+                add_cell<false>(acc, pe, pa, C.g[a], C.g[b], nbb, w4, W1, s_A2[a] * s_A1[b]);
+            if (a != b)
+            {
+                // (b, a): the inverse kernel swaps partner species
+                // (kernel_pair.hpp:200-216)
+                const double qe[4] = {pe[1], pe[0], pe[3], pe[2]};
+                const double qa[4] = {pa[1], pa[0], pa[3], pa[2]};
+                if (L.stim)
+                    add_cell<true>(acc, qe, qa, C.g[b], C.g[a], nbb, w4, W1, s_A2[b] * s_A1[a]);
+                else
+                    add_cell<false>(acc, qe, qa, C.g[b], C.g[a], nbb, w4, W1, s_A2[b] * s_A1[a]);
+            }
+        }
+#pragma unroll
+        for (int kk = 0; kk < 16; ++kk)
+            acc[kk] = warp_sum(acc[kk]);
+        if (lane == 0)
+        {
+#pragma unroll
+            for (int kk = 0; kk < 16; ++kk)
+                P->s2d[kk] = acc[kk];
+        }
+    }
+}
+
+// IMPL: 0 HR98, 1 BRT06, 2 GP19.  ADD: accumulate onto the pair sums.
+template <bool MIXED, int IMPL>
+__global__ void __launch_bounds__(kWarps * 32)
+    grey_brem_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
+                     double* __restrict__ scratch, int add)
+{
+    __shared__ double s_A1[kMaxM], s_A2[kMaxM];
+    __shared__ uint32_t s_cells[kMaxCells];
+    __shared__ CellTab s_ct[kWarps];
+    for (int k = threadIdx.x; k < kMaxM; k += blockDim.x)
+    {
+        s_A1[k] = L.A1[k];
+        s_A2[k] = L.A2[k];
+    }
+    for (int k = threadIdx.x; k < L.ncell; k += blockDim.x)
+        s_cells[k] = L.cells[k];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    CellTab& C     = s_ct[threadIdx.x >> 5];
+    const int M    = 2 * L.n2;
+    const bool nbb = L.neglect_blocking != 0;
+    const int64_t nwarp = (int64_t)gridDim.x * kWarps;
+    const Gp19Table G19 = {L.gp19.d0, L.gp19.d1, L.gp19.d2,    L.gp19.d3,   L.gp19.nb,  L.gp19.ye,
+                           L.gp19.t,  L.gp19.w,  L.gp19.lognb, L.gp19.logw, L.gp19.data};
+
+    for (int64_t q = (int64_t)blockIdx.x * kWarps + (threadIdx.x >> 5); q < np; q += nwarp)
+    {
+        const int64_t p = p0 + q;
+        PointTab* P     = (PointTab*)(scratch + q * kTabWords);
+        const double T  = L.eos[1][p];
+        __syncwarp();
+        load_cell_tab(C, P, M, false, lane);
+        if (IMPL == 0)
+        {
+            warp_copy((double*)&C.hr, (const double*)&P->hr, sizeof(Hr98Point) / sizeof(double),
+                      lane);
+            __syncwarp();
+            if (MIXED && lane == 0)
+                fp32::hr98_mixed_from(C.hr, &C.hm);
+        }
+        __syncwarp();
+        double acc[16];
+#pragma unroll
+        for (int kk = 0; kk < 16; ++kk)
+            acc[kk] = 0.;
+        const double nbp = L.eos[0][p], yep = L.eos[2][p];
+        for (int c = lane; c < L.ncell; c += 32)
+        {
+            const uint32_t ab = s_cells[c];
+            const int a = ab & 0xffffu, b = ab >> 16;
+            const double nua = C.nu[a], nub = C.nu[b];
+            double be, ba;
+            if (IMPL == 0)
+            {
+                if (MIXED)
+                {
+                    const double x   = (nua + nub) / T;
+                    const float xf   = (float)x;
+                    const float xlo  = (float)(x - (double)xf);
+                    const double sab = C.hm.outer * (double)fp32::hr98_shape(C.hm, xf);
+                    ba = sab;
+                    // e^{-x} = e^{-xf} (1 - xlo): keeps the argument's FP64 bits
+                    be = sab * (double)(expf(-xf) * (1.f - xlo));
+                }
+                else
+                    hr98_kernel(C.hr, nua, nub, &be, &ba);
+            }
+            else if (IMPL == 1)
+                brt06_kernel(C.brt06_pre, T, nua, nub, &be, &ba);
+            else
+                gp19_kernel(G19, nbp, yep, T, nua, nub, &be, &ba);
+            const double Kem[4] = {be, be, be, be};
+            const double Kab[4] = {ba, ba, ba, ba};
+            const double w4 = (nua * nua) * (nub * nub);
+            const double W1 = s_A1[a] * s_A1[b];
+            if (L.stim)
+                add_cell<true>(acc, Kem, Kab, C.g[a], C.g[b], nbb, w4, W1, s_A2[a] * s_A1[b]);
+            else
+                add_cell<false>(acc, Kem, Kab, C.g[a], C.g[b], nbb, w4, W1, s_A2[a] * s_A1[b]);
+            if (a != b)
+            {
+                if (L.stim)
+                    add_cell<true>(acc, Kem, Kab, C.g[b], C.g[a], nbb, w4, W1, s_A2[b] * s_A1[a]);
+                else
+                    add_cell<false>(acc, Kem, Kab, C.g[b], C.g[a], nbb, w4, W1,
+                                    s_A2[b] * s_A1[a]);
+            }
+        }
+#pragma unroll
+        for (int kk = 0; kk < 16; ++kk)
+            acc[kk] = warp_sum(acc[kk]);
+        if (lane == 0)
+        {
+#pragma unroll
+            for (int kk = 0; kk < 16; ++kk)
+                P->s2d[kk] = add ? P->s2d[kk] + acc[kk] : acc[kk];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// NES / NPS (m1_opacities.hpp:864-1057, integration.hpp:687-768)
+// ---------------------------------------------------------------------------
+struct NepsTab
+{
+    Distr d;
+    double fe[2][6];
+    double fd0[2];
+    double same_cf;
+};
+
+__global__ void __launch_bounds__(kWarps * 32)
+    grey_neps_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
+                     double* __restrict__ scratch)
+{
+    __shared__ double s_x2[kMaxQ], s_w2[kMaxQ], s_wx[kMaxQ], s_wx3[kMaxQ];
+    __shared__ NepsTab s_nt[kWarps];
+    for (int k = threadIdx.x; k < kMaxQ; k += blockDim.x)
+    {
+        s_x2[k]  = L.x2[k];
+        s_w2[k]  = L.w2[k];
+        s_wx[k]  = L.wx[k];
+        s_wx3[k] = L.wx3[k];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    NepsTab& N     = s_nt[threadIdx.x >> 5];
+    const int n2   = L.n2;
+    const bool nbb = L.neglect_blocking != 0;
+    const int64_t nwarp = (int64_t)gridDim.x * kWarps;
+
+    for (int64_t q = (int64_t)blockIdx.x * kWarps + (threadIdx.x >> 5); q < np; q += nwarp)
+    {
+        const int64_t p = p0 + q;
+        PointTab* P     = (PointTab*)(scratch + q * kTabWords);
+        const double T  = L.eos[1][p], mu_e = L.eos[7][p];
+        __syncwarp();
+        warp_copy((double*)&N.d, (const double*)&P->d, 28 + 12 + 2, lane);
+        if (lane == 0)
+            N.same_cf = P->same_cf;
+        __syncwarp();
+        const bool same_cf = N.same_cf != 0.;
+        NepsPoint NP;
+        NP.T    = T;
+        NP.pre  = k::NepsConst * (T * T);
+        NP.eta0 = mu_e / T;
+        NP.eta1 = -mu_e / T;
+        NP.fd00 = N.fd0[0];
+        NP.fd01 = N.fd0[1];
+        NP.fe0  = N.fe[0];
+        NP.fe1  = N.fe[1];
+        const double tn = 4. * (k::TempMultiple * T);
+        double acc[16];
+#pragma unroll
+        for (int kk = 0; kk < 16; ++kk)
+            acc[kk] = 0.;
+        const int nn2 = n2 * n2;
+        for (int it = lane; it < 2 * nn2; it += 32)
+        {
+            const int r   = it >= nn2;
+            const int rem = it - r * nn2;
+            const int i = rem / n2, j = rem - (rem / n2) * n2;
+            const double xi = s_x2[i], xj = s_x2[j];
+            double nu, nub;
+            if (!r)
+            {
+                nu  = 0.5 * tn * xi * (1. - xj);
+                nub = 0.5 * tn * xi * (1. + xj);
+            }
+            else
+            {
+                nu  = 0.5 * tn * (1. - xj) / xi;
+                nub = 0.5 * tn * (1. + xj) / xi;
+            }
+            const double w4 = (nu * nu) * (nub * nub);
+            double g[4], gb[4];
+            total_nu_f4(nu, N.d, same_cf, g);
+            total_nu_f4(nub, N.d, same_cf, gb);
+            double em1[4], ab1[4], em2[4], ab2[4];
+            neps_pair(NP, nu, nub, em1, ab1, em2, ab2);
+            const double Wr = (r ? s_wx3[i] : s_wx[i]) * s_w2[j];
+#pragma unroll
+            for (int s = 0; s < 4; ++s)
+            {
+                const double e1 = em1[s] * gb[s];
+                const double a1 = ab1[s] * (nbb ? 1. : 1. - gb[s]);
+                const double e2 = em2[s] * g[s];
+                const double a2 = ab2[s] * (nbb ? 1. : 1. - g[s]);
+                double EM1, AB1, EM2, AB2;
+                if (L.stim)
+                {
+                    AB1 = w4 * g[s] * (e1 + a1);
+                    EM1 = w4 * e1;
+                    AB2 = w4 * gb[s] * (e2 + a2);
+                    EM2 = w4 * e2;
+                }
+                else
+                {
+                    AB1 = w4 * g[s] * a1;
+                    EM1 = w4 * (1. - g[s]) * e1;
+                    AB2 = w4 * gb[s] * a2;
+                    EM2 = w4 * (1. - gb[s]) * e2;
+                }
+                acc[s] += Wr * (EM1 + EM2);
+                acc[4 + s] += Wr * (AB1 + AB2);
+                acc[8 + s] += Wr * (nu * EM1 + nub * EM2);
+                acc[12 + s] += Wr * (nu * AB1 + nub * AB2);
+            }
+        }
+#pragma unroll
+        for (int kk = 0; kk < 16; ++kk)
+            acc[kk] = warp_sum(acc[kk]);
+        if (lane == 0)
+        {
+#pragma unroll
+            for (int kk = 0; kk < 16; ++kk)
+                P->snes[kk] = acc[kk];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// assembly (m1_opacities.hpp:1172-1294), one thread per point
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128)
+    grey_final_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
+                      const double* __restrict__ scratch)
+{
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < np;
+         q += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int64_t p     = p0 + q;
+        const PointTab* P   = (const PointTab*)(scratch + q * kTabWords);
+        const double T      = L.eos[1][p];
+        const double eta_e  = L.eos[7][p] / T;
+        const double t2d    = k::TempMultiple * T;
+        const double t2     = t2d * t2d;
+        const double tn     = 4. * (k::TempMultiple * T);
+        const double hn     = 0.5 * (tn * tn);
+        const bool has2d    = L.use_pair || L.use_brem;
+        double sb[2];
+        double fe[2][6];
+#pragma unroll
+        for (int e = 0; e < 2; ++e)
+#pragma unroll
+            for (int kk = 0; kk < 6; ++kk)
+                fe[e][kk] = P->fe[e][kk];
+        beta_scales(T, eta_e, fe, sb);
+        const double F = k::FourPiHc3, F2 = k::FourPiHc3Sqr, c = k::Clight;
+#pragma unroll
+        for (int s = 0; s < 4; ++s)
+        {
+            const double n = L.m1[s][p], J = L.m1[4 + s][p];
+            const double s_iso = (n > k::ThresholdN) ? (J / n) : 1.5 * T;
+            const double n2d_em = has2d ? P->s2d[s] * t2 : 0.;
+            const double n2d_ab = has2d ? P->s2d[4 + s] * t2 : 0.;
+            const double e2d_em = has2d ? P->s2d[8 + s] * t2d * t2 : 0.;
+            const double e2d_ab = has2d ? P->s2d[12 + s] * t2d * t2 : 0.;
+            const double nne_em = L.use_inel ? P->snes[s] * hn : 0.;
+            const double nne_ab = L.use_inel ? P->snes[4 + s] * hn : 0.;
+            const double ene_em = L.use_inel ? P->snes[8 + s] * hn : 0.;
+            const double ene_ab = L.use_inel ? P->snes[12 + s] * hn : 0.;
+            const double iso    = L.use_iso ? P->siso[s] * s_iso : 0.;
+            double o[5];
+            if (s < 2)
+            {
+                double bne = 0., bje = 0., bna = 0., bja = 0.;
+                if (L.use_abs_em)
+                {
+                    bne = P->sbeta[s] * sb[s];
+                    bje = P->sbeta[2 + s] * sb[s];
+                    bna = P->sbeta[4 + s] * sb[s];
+                    bja = P->sbeta[6 + s] * sb[s];
+                }
+                o[0] = F * (F * (n2d_em + nne_em) + bne);
+                o[2] = F * (F * (e2d_em + ene_em) + bje);
+                o[1] = (n > k::ThresholdN) ? F / (c * n) * (F * (n2d_ab + nne_ab) + bna) : 0.;
+                o[3] = (J > k::ThresholdJ) ?
+                           ((s == 0 && n == 0.) ? 0. : F / (c * J) * (F * (e2d_ab + ene_ab) + bja)) :
+                           0.;
+            }
+            else
+            {
+                o[0] = F2 * (n2d_em + nne_em);
+                o[2] = F2 * (e2d_em + ene_em);
+                o[1] = (n > k::ThresholdN) ?
+                           ((s == 3 && n == 0.) ? 0. : F2 / (c * n) * (n2d_ab + nne_ab)) :
+                           0.;
+                o[3] = (J > k::ThresholdJ) ? F2 / (c * J) * (e2d_ab + ene_ab) : 0.;
+            }
+            o[4] = (J > k::ThresholdJ) ? F / (c * J) * iso : 0.;
+#pragma unroll
+            for (int qq = 0; qq < 5; ++qq)
+                L.out[qq * 4 + s][p] = o[qq];
+        }
+    }
+}
+
+template <class K>
+int grid_for(K kernel, int threads, int64_t work, int num_sms)
+{
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) !=
+            cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    const int64_t cap = (int64_t)num_sms * per_sm;
+    return (int)(work < cap ? (work > 0 ? work : 1) : cap);
+}
+
+template <bool MIXED>
+cudaError_t launch_brem(const OpacityLaunch& L, int64_t p0, int64_t np, double* ws,
+                        cudaStream_t st, int sms, int add)
+{
+    const int64_t wb = (np + kWarps - 1) / kWarps;
+    if (L.brem_impl == 0)
+        grey_brem_kernel<MIXED, 0>
+            <<<grid_for(grey_brem_kernel<MIXED, 0>, kWarps * 32, wb, sms), kWarps * 32, 0, st>>>(
+                L, p0, np, ws, add);
+    else if (L.brem_impl == 1)
+        grey_brem_kernel<MIXED, 1>
+            <<<grid_for(grey_brem_kernel<MIXED, 1>, kWarps * 32, wb, sms), kWarps * 32, 0, st>>>(
+                L, p0, np, ws, add);
+    else
+        grey_brem_kernel<MIXED, 2>
+            <<<grid_for(grey_brem_kernel<MIXED, 2>, kWarps * 32, wb, sms), kWarps * 32, 0, st>>>(
+                L, p0, np, ws, add);
+    return cudaGetLastError();
+}
+
+} // namespace
+
+cudaError_t launch_grey(const OpacityLaunch& L, cudaStream_t st, int sms, double* ws,
+                        int64_t ws_points)
+{
+    if (L.npts <= 0)
+        return cudaSuccess;
+    if (!ws || ws_points < 1)
+        return cudaErrorInvalidValue;
+    for (int64_t p0 = 0; p0 < L.npts; p0 += ws_points)
+    {
+        const int64_t np = (L.npts - p0) < ws_points ? (L.npts - p0) : ws_points;
+        const int64_t wb = (np + kWarps - 1) / kWarps;
+        grey_prelude_kernel<<<grid_for(grey_prelude_kernel, kWarps * 32, wb, sms), kWarps * 32, 0,
+                              st>>>(L, p0, np, ws);
+        if (L.use_pair)
+        {
+            if (L.mixed)
+                grey_pair_kernel<true><<<grid_for(grey_pair_kernel<true>, kWarps * 32, wb, sms),
+                                         kWarps * 32, 0, st>>>(L, p0, np, ws);
+            else
+                grey_pair_kernel<false><<<grid_for(grey_pair_kernel<false>, kWarps * 32, wb, sms),
+                                          kWarps * 32, 0, st>>>(L, p0, np, ws);
+        }
+        if (L.use_brem)
+        {
+            cudaError_t e = L.mixed ? launch_brem<true>(L, p0, np, ws, st, sms, L.use_pair) :
+                                      launch_brem<false>(L, p0, np, ws, st, sms, L.use_pair);
+            if (e != cudaSuccess)
+                return e;
+        }
+        if (L.use_inel)
+            grey_neps_kernel<<<grid_for(grey_neps_kernel, kWarps * 32, wb, sms), kWarps * 32, 0,
+                               st>>>(L, p0, np, ws);
+        grey_final_kernel<<<grid_for(grey_final_kernel, 128, (np + 127) / 128, sms), 128, 0, st>>>(
+            L, p0, np, ws);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess)
+            return e;
+    }
+    return cudaSuccess;
+}
+
+} // namespace bnsn

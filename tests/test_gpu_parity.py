@@ -224,11 +224,18 @@ def test_spectral_many_energies_chunked(cuda, port, port_fma):
     assert_close(out.cpu().numpy(), want, pr, what="spectral 100 energies")
 
 
-def test_distr_and_equilibrium_vs_oracle(cuda, port):
+def test_distr_and_equilibrium_vs_oracle(cuda, port, port_fma):
     eos, m1 = bn.synthetic_points(3, 2000)
     m = cuda.from_numpy(m1).cuda()
     got = bn.distr_from_m1(m).cpu().numpy()
-    assert_close(got, port.distr_from_m1(eos, m1), what="distr_from_m1")
+    # eta_t is a rational fit in y = n^4/J^3 (with log/exp); its conditioning
+    # is probed by the FMA build and by +2 ulp in n and in J
+    m1a, m1b = m1.copy(), m1.copy()
+    m1a[0:4] *= 1. + 2. ** -51
+    m1b[4:8] *= 1. + 2. ** -51
+    pr = [port_fma.distr_from_m1(eos, m1), port.distr_from_m1(eos, m1a),
+          port.distr_from_m1(eos, m1b)]
+    assert_close(got, port.distr_from_m1(eos, m1), pr, what="distr_from_m1")
     d, mm = bn.nu_equilibrium(cuda.from_numpy(eos).cuda())
     dw, mw = port.nu_equilibrium(eos)
     assert_close(d.cpu().numpy(), dw, what="equilibrium distr")
@@ -265,7 +272,7 @@ def test_gp19_requires_table(cuda):
     got = gpu_grey(cuda, eos, m1, (0, 0, 1, 0, 0), (1, 0, 1, 1, 1, 2, 1, 0), 6)
     assert np.isfinite(got).all()
     assert lib.bnsn_status_string(C.ERR_NO_TABLE) == b"GP19 table not loaded"
-    assert ctypes.sizeof(C.OpacityParams) == 12
+    assert ctypes.sizeof(C.OpacityParams) == 16
 
 
 def test_full_size_subsample_parity(cuda, port, port_fma):
