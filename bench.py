@@ -1,22 +1,38 @@
 """Benchmark of the grey M1 opacity path on GB300.
 
-One step = the grey M1 opacities (ComputeM1Opacities semantics, all 20
-outputs, 4 species) of every point of the workload, one kernel launch.
+Metric: grey M1 opacity points/s of the mixed-precision path, with the plain
+FP64 GPU path timed on the same points and the mixed-vs-FP64 relative error
+reported beside it.
 
-  value : points/s with inputs and outputs resident in HBM, device time of K
-          launches between CUDA events (max over ranks).
-  e2e   : points/s through the host-buffer C-ABI call bnsn_m1_opacities_host
-          (pinned host buffers, host->device and device->host copies inside
-          the timed region).
-  roofline / cpu_baseline / clocks / gpu_launches: see the design doc.
+One step = the grey M1 opacities (ComputeM1Opacities semantics: all 20
+outputs, 4 species, stimulated absorption) of one batch of points:
 
-Workloads (synthetic, seeded; the reference's inputs are CCSN/BNS tables):
-  c2  : 128^3 = 2,097,152 points, beta + iso + pair + HR98, n = 10
-  c5  : 256^3 = 16,777,216 points, all reactions, GP19 (synthetic table), n = 20
-  c1  : 4096 points, beta + iso + pair + HR98, n = 10
+  c5 (default) : 256^3 all-reactions workload (beta with weak magnetism and
+                 mean-field shift, iso scattering, e+e- pair, GP19 brem on the
+                 synthetic table, NES/NPS), n = 20.  A step is one
+                 256 x 256 x 16 slab = 1,048,576 points.
+  c3           : the 128^3 patch, beta + iso + pair + HR98, n = 10 (whole patch).
+  c2           : as c3 (the FP64 configuration of the same patch).
+  c1           : 4096 points, beta + iso + pair + HR98, n = 10.
 
-``--impl reference`` times the reference algorithm on the host cores (the
-CPU oracle, oracle/) for the same workload on a bounded sample per step.
+Keys of the JSON line:
+  value        : points/s of --precision (default mixed) with inputs and outputs
+                 resident in HBM; CUDA events around K steps (max over ranks).
+  fp64_gpu     : the plain FP64 path on the same points (--precision mixed).
+  accuracy     : max / p99 relative error of mixed vs FP64 over every output.
+  e2e          : points/s through the host-buffer C-ABI call
+                 bnsn_m1_opacities_host (pinned host buffers, host<->device
+                 copies inside the timed region).
+  roofline     : the kernel phase with the largest device time, its FP64 work
+                 per point from an ncu instruction count
+                 (profiles/bench_constants.json) over its event-timed duration,
+                 against the FP64 peak measured in this run by a DFMA probe.
+  cpu_baseline : the reference algorithm (C restatement in oracle/, pinned
+                 bit-for-bit to the reference build) on all host cores, on a
+                 bounded sample of the same points.
+
+``--impl reference`` times that CPU implementation alone on the same workload,
+each step a bounded sample.
 """
 
 import argparse
@@ -34,16 +50,18 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 SEED = 20261203
+BREM_NAMES = ["HR98", "BRT06", "GP19"]
 WORKLOADS = {
-    "c1": dict(npts=4096, flags=(1, 1, 1, 0, 1), brem=0, nq=10),
-    "c2": dict(npts=128 ** 3, flags=(1, 1, 1, 0, 1), brem=0, nq=10),
-    "c5": dict(npts=256 ** 3, flags=(1, 1, 1, 1, 1), brem=2, nq=20),
+    "c1": dict(npts=4096, flags=(1, 1, 1, 0, 1), brem=0, nq=10,
+               desc="4096 points, beta+iso+pair+HR98, n=10"),
+    "c2": dict(npts=128 ** 3, flags=(1, 1, 1, 0, 1), brem=0, nq=10,
+               desc="128^3 = 2,097,152 points, beta+iso+pair+HR98, n=10"),
+    "c3": dict(npts=128 ** 3, flags=(1, 1, 1, 0, 1), brem=0, nq=10,
+               desc="128^3 = 2,097,152 points, beta+iso+pair+HR98, n=10"),
+    "c5": dict(npts=256 * 256 * 16, flags=(1, 1, 1, 1, 1), brem=2, nq=20,
+               desc="256^3 all reactions (beta+WM+mean field, iso, pair, GP19 brem, NES/NPS), "
+                    "n=20; one step = one 256x256x16 slab = 1,048,576 points"),
 }
-# Per-point FP64 work of the grey kernel, in FLOP (a DFMA counts 2), from an
-# ncu count of the kernel's FP64 instructions over a sample of the workload
-# (profiles/grey_fp64_c2.md); the kernel evaluates each distinct quantity
-# once, so this is the algorithm's work, not repeated work.
-FP64_FLOP_PER_POINT = {"c2": None, "c5": None, "c1": None}
 
 
 def parse():
@@ -52,12 +70,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--npts", type=int, default=0, help="override the point count")
-    ap.add_argument("--cpu-sample", type=int, default=16384)
+    ap.add_argument("--workload", default="c5", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--npts", type=int, default=0, help="override the points per step")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0,
+                    help="target CPU time of the cpu_baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison")
     return ap.parse_args()
 
 
@@ -125,35 +145,37 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def load_peaks():
+def load_json(*path):
     try:
-        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+        with open(os.path.join(REPO, *path)) as f:
             return json.load(f)
     except OSError:
         return {}
 
 
-def load_profile_numbers():
-    """FP64 FLOP/point and DRAM bytes/point recorded from ncu (profiles/)."""
-    try:
-        with open(os.path.join(REPO, "profiles", "bench_constants.json")) as f:
-            return json.load(f)
-    except OSError:
-        return {}
-
-
-def cpu_sample_rate(eos, m1, wl, nsample, nthreads):
-    """Reference algorithm (CPU oracle, restatement of the reference C++) on
-    host cores: points/s over a bounded sample of the workload."""
+def cpu_rate(eos, m1, wl, n, nthreads):
+    """Reference algorithm (oracle/ C restatement) on host cores: points/s."""
     import oracle
     port = oracle.port()
     q = port.gauss_legendre(wl["nq"])
     pars = (1, 0, 1, 1, 1, wl["brem"], 1, 0)
-    idx = slice(0, nsample)
     t0 = time.perf_counter()
-    port.m1_opacities(eos[:, idx], m1[:, idx], wl["flags"], pars, q, nthreads=nthreads)
+    port.m1_opacities(eos[:, :n], m1[:, :n], wl["flags"], pars, q, nthreads=nthreads)
     dt = time.perf_counter() - t0
-    return nsample / dt, dt
+    return n / dt, dt
+
+
+def cpu_sample_size(eos, m1, wl, seconds, nthreads, cap):
+    """Points the CPU processes in about `seconds` (pilot of 8 points/thread)."""
+    pilot = min(cap, 8 * nthreads)
+    rate, _ = cpu_rate(eos, m1, wl, pilot, nthreads)
+    return int(max(pilot, min(cap, rate * seconds)))
+
+
+def setup_gp19(bn, wl):
+    if wl["brem"] == 2:
+        from bns_nurates_gb300 import gp19_synthetic
+        bn.set_gp19_table(gp19_synthetic.table())
 
 
 def run_reference(args, rank, world):
@@ -164,31 +186,53 @@ def run_reference(args, rank, world):
     import bns_nurates_gb300 as bn
     from bns_nurates_gb300 import build as libbuild
     libbuild.build()
-    wl = WORKLOADS[args.workload]
+    wl = dict(WORKLOADS[args.workload])
     nthreads = os.cpu_count()
-    n = args.cpu_sample
-    eos, m1 = bn.synthetic_points(SEED, n)
+    cap = min(wl["npts"], 1 << 18)
+    eos, m1 = bn.synthetic_points(SEED, cap)
+    per_step = max(2.0, min(args.cpu_seconds, 150.0 / max(1, args.steps + args.warmup)))
+    n = cpu_sample_size(eos, m1, wl, per_step, nthreads, cap)
     for _ in range(args.warmup):
-        cpu_sample_rate(eos, m1, wl, min(n, 512), nthreads)
-    rates = []
-    for _ in range(args.steps):
-        r, _ = cpu_sample_rate(eos, m1, wl, n, nthreads)
-        rates.append(r)
+        cpu_rate(eos, m1, wl, min(n, 4 * nthreads), nthreads)
+    rates = [cpu_rate(eos, m1, wl, n, nthreads)[0] for _ in range(args.steps)]
     value = statistics.median(rates)
+    sample = f"first {n} points of the {args.workload} workload per step"
     line = {
         "impl": "reference", "metric": "grey M1 opacity points/s", "value": value,
         "unit": "points/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * n / value, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
-        "config": {"workload": f"{args.workload}: sample of {n} points per step",
-                   "reactions": wl["flags"], "brem": ["HR98", "BRT06", "GP19"][wl["brem"]],
-                   "nquad": wl["nq"]},
+        "config": {"workload": wl["desc"], "sample_points_per_step": n,
+                   "reactions": wl["flags"], "brem": BREM_NAMES[wl["brem"]], "nquad": wl["nq"],
+                   "precision": "fp64 (reference CPU algorithm)"},
         "cpu_baseline": {"value": value, "unit": "points/s", "cores": nthreads, "kind": "port",
-                         "sample": f"{n} points of the {args.workload} workload per step"},
+                         "sample": sample},
         "e2e": {"value": value, "unit": "points/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
+
+
+def rel_err(a, b):
+    """|a - b| / |b| elementwise, 0 where both are equal (including zeros)."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        r = np.abs(a - b) / np.abs(b)
+    r[a == b] = 0.
+    r[~np.isfinite(r)] = np.inf
+    return r
+
+
+def timed_steps(step, steps, stream, torch):
+    """Device ms of `steps` calls between events on `stream`."""
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0.record(stream)
+    for _ in range(steps):
+        step()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    return t0.elapsed_time(t1)
 
 
 def main():
@@ -218,53 +262,63 @@ def main():
     q = bn.gauss_legendre(wl["nq"])
     flags = bn.opacity_flags(*wl["flags"])
     params = bn.opacity_params(brem_implementation=wl["brem"])
-    if wl["brem"] == 2:
-        from bns_nurates_gb300 import gp19_synthetic
-        bn.set_gp19_table(gp19_synthetic.table())
+    setup_gp19(bn, wl)
+    warmup = max(args.warmup, 3)
 
     # per-rank shard of points (weak scaling): rank r owns points [r n, (r+1) n)
+    from bns_nurates_gb300 import shards
+    first, _ = shards.rank_points(n, rank)
     t0 = time.perf_counter()
-    eos_h, m1_h = bn.synthetic_points(SEED, n, first=rank * n)
+    eos_h, m1_h = bn.synthetic_points(SEED, n, first=first)
     gen_s = time.perf_counter() - t0
     eos = torch.from_numpy(eos_h).to(dev)
     m1 = torch.from_numpy(m1_h).to(dev)
     out = torch.empty((20, n), dtype=torch.float64, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    def step():
-        bn.m1_opacities(eos, m1, flags, params, q, out=out, precision=args.precision,
-                        stream=stream)
+    def step(precision=args.precision, o=out):
+        bn.m1_opacities(eos, m1, flags, params, q, out=o, precision=precision, stream=stream)
 
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(warmup):
         step()
     torch.cuda.synchronize()
 
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    # timed region: K steps, per-phase events around every kernel launch
     if world > 1:
         torch.distributed.barrier()
-    torch.cuda.synchronize()
+    bn.phase_times()
+    bn.phase_timing(True)
+    launches0 = bn.kernel_launches()
     with ClockSampler(local) as clk:
-        t_all0 = torch.cuda.Event(enable_timing=True)
-        t_all1 = torch.cuda.Event(enable_timing=True)
-        t_all0.record(stream)
-        for k in range(args.steps):
-            starts[k].record(stream)
-            step()
-            ends[k].record(stream)
-        t_all1.record(stream)
-        torch.cuda.synchronize()
+        total_ms = timed_steps(step, args.steps, stream, torch)
+    launches = bn.kernel_launches() - launches0
+    bn.phase_timing(False)
+    phases = bn.phase_times()
     if world > 1:
         torch.distributed.barrier()
-    total_ms = t_all0.elapsed_time(t_all1)
-    launch_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    if world > 1:
-        tt = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(tt.item())
+        total_ms = shards.max_over_ranks(total_ms, dev)
     ms_per_step = total_ms / args.steps
     value = world * n / (ms_per_step * 1e-3)
     assert torch.isfinite(out).all().item(), "non-finite outputs"
+    res = out.cpu().numpy()
+
+    # plain FP64 GPU path on the same points
+    fp64 = accuracy = None
+    if args.precision == "mixed" and not args.no_fp64:
+        out64 = torch.empty_like(out)
+        step("fp64", out64)
+        k64 = max(1, min(2, args.steps))
+        ms64 = timed_steps(lambda: step("fp64", out64), k64, stream, torch) / k64
+        fp64 = {"value": world * n / (ms64 * 1e-3), "unit": "points/s", "ms_per_step": ms64,
+                "steps": k64, "warmup": 1, "mixed_over_fp64": ms64 / ms_per_step}
+        r = rel_err(res, out64.cpu().numpy())
+        names = [f"{f}[{s}]" for f in ("eta_0", "kappa_0_a", "eta", "kappa_a", "kappa_s")
+                 for s in ("nue", "anue", "nux", "anux")]
+        accuracy = {"vs": "plain FP64 GPU path, every output of every point",
+                    "max_rel": float(r.max()), "p99_rel": float(np.percentile(r, 99)),
+                    "p999_rel": float(np.percentile(r, 99.9)),
+                    "frac_above_1e-6": float(np.mean(r > 1e-6)),
+                    "max_rel_per_output": {nm: float(r[k].max()) for k, nm in enumerate(names)}}
 
     # end to end through the host-buffer C-ABI call, pinned host memory
     e2e = None
@@ -274,7 +328,7 @@ def main():
         out_p = torch.empty((20, n), dtype=torch.float64).pin_memory()
         e_np, m_np, o_np = eos_p.numpy(), m1_p.numpy(), out_p.numpy()
         bn.m1_opacities_host(e_np, m_np, flags, params, q, out=o_np, precision=args.precision)
-        ksteps = max(1, min(args.steps, 3))
+        ksteps = max(1, min(args.steps, 2))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(ksteps):
@@ -282,61 +336,75 @@ def main():
                                  precision=args.precision)
         dt = (time.perf_counter() - t0) / ksteps
         if world > 1:
-            tt = torch.tensor([dt], device=dev)
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            dt = float(tt.item())
+            dt = shards.max_over_ranks(dt, dev)
         e2e = {"value": world * n / dt, "unit": "points/s",
-               "h2d_bytes_per_step": int(23 * 8 * n), "d2h_bytes_per_step": int(20 * 8 * n)}
-        assert np.array_equal(o_np, out.cpu().numpy()), "host and device paths differ"
+               "h2d_bytes_per_step": int(23 * 8 * n), "d2h_bytes_per_step": int(20 * 8 * n),
+               "call": "bnsn_m1_opacities_host"}
+        assert np.array_equal(o_np, res), "host-buffer and device paths differ"
 
-    peaks = load_peaks()
-    prof = load_profile_numbers().get(args.workload, {})
-    kernel_ms = statistics.median(launch_ms)
-    flop_pt = prof.get("fp64_flop_per_point")
+    # roofline of the dominant kernel phase
+    peaks = load_json("MEASURED_PEAKS.json")
+    consts = load_json("profiles", "bench_constants.json").get(args.workload, {}).get(
+        args.precision, {})
+    top = max(phases, key=lambda k: phases[k][0])
+    top_ms, top_launches = phases[top]
     fp64_peak = bn.fp64_peak_tflops()
-    roofline = {"bound": "fp64", "unit": "TFLOP/s", "achieved": None, "peak": fp64_peak,
-                "frac": None, "traffic": None,
-                "peak_source": "measured in this run: DFMA-chain probe (bnsn_fp64_peak_probe)"}
-    if flop_pt:
-        ach = flop_pt * n / (kernel_ms * 1e-3) / 1e12
+    c = consts.get(top, {})
+    pts_per_launch = n * args.steps / max(1, top_launches)
+    roofline = {"kernel": f"grey phase '{top}'", "bound": "fp64", "unit": "TFLOP/s",
+                "achieved": None, "peak": fp64_peak, "frac": None, "traffic": None,
+                "peak_source": "FP64 DFMA-chain probe run in this process "
+                               "(bnsn_fp64_peak_probe); not in MEASURED_PEAKS.json",
+                "launch_ms": top_ms / max(1, top_launches), "launches": top_launches,
+                "share_of_step": top_ms / total_ms if total_ms else None}
+    if c.get("fp64_flop_per_point"):
+        ach = c["fp64_flop_per_point"] * pts_per_launch / (roofline["launch_ms"] * 1e-3) / 1e12
         roofline["achieved"] = ach
-        if fp64_peak:
-            roofline["frac"] = ach / fp64_peak
-    if prof.get("dram_bytes_per_point"):
-        roofline["traffic"] = prof["dram_bytes_per_point"] * n
+        roofline["frac"] = ach / fp64_peak if fp64_peak else None
+        roofline["work_source"] = c.get("source")
+    if c.get("dram_bytes_per_point"):
+        roofline["traffic"] = c["dram_bytes_per_point"] * pts_per_launch
+    if c.get("fp32_flop_per_point"):
+        roofline["fp32_tflops"] = (c["fp32_flop_per_point"] * pts_per_launch /
+                                   (roofline["launch_ms"] * 1e-3) / 1e12)
     hbm = peaks.get("hbm_gbs")
-    alg_bytes = (23 + 20) * 8 * n
-    roofline["hbm"] = {"achieved_gbs": alg_bytes / (kernel_ms * 1e-3) / 1e9,
-                       "peak_gbs": hbm, "frac": (alg_bytes / (kernel_ms * 1e-3) / 1e9 / hbm)
-                       if hbm else None, "note": "secondary: algorithmic I/O bytes only"}
+    io_gbs = (23 + 20) * 8 * n / (ms_per_step * 1e-3) / 1e9
+    roofline["hbm_secondary"] = {"achieved_gbs": io_gbs, "peak_gbs": hbm,
+                                 "frac": io_gbs / hbm if hbm else None,
+                                 "note": "algorithmic I/O bytes (23 inputs + 20 outputs "
+                                         "x 8 B per point) over the step time"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         import oracle
         oracle.build()
-        ns = min(args.cpu_sample, n)
-        rate, dt = cpu_sample_rate(eos_h, m1_h, wl, ns, os.cpu_count())
-        cpu = {"value": rate, "unit": "points/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"first {ns} points of the workload, {dt:.1f} s"}
+        nthreads = os.cpu_count()
+        ns = cpu_sample_size(eos_h, m1_h, wl, args.cpu_seconds, nthreads, n)
+        rate, dt = cpu_rate(eos_h, m1_h, wl, ns, nthreads)
+        cpu = {"value": rate, "unit": "points/s", "cores": nthreads, "kind": "port",
+               "sample": f"first {ns} points of the step's batch, {dt:.1f} s"}
 
     if rank == 0:
         line = {
-            "metric": "grey M1 opacity points/s", "value": value, "unit": "points/s",
-            "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
+            "metric": "grey M1 opacity points/s, mixed vs FP64 GPU",
+            "value": value, "unit": "points/s",
+            "n_gpus": world, "steps": args.steps, "warmup": warmup,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
-            "data": "synthetic (seeded generator, reference-shaped inputs)",
-            "config": {"workload": f"{args.workload}: {n} points per GPU",
+            "data": "synthetic (seeded generator with the reference's input ranges)",
+            "config": {"workload": wl["desc"], "points_per_step_per_gpu": n,
                        "reactions": {"abs_em": wl["flags"][0], "pair": wl["flags"][1],
                                      "brem": wl["flags"][2], "inelastic": wl["flags"][3],
                                      "iso": wl["flags"][4]},
-                       "brem": ["HR98", "BRT06", "GP19"][wl["brem"]], "nquad": wl["nq"],
+                       "brem": BREM_NAMES[wl["brem"]], "nquad": wl["nq"],
                        "precision": args.precision, "stim_abs": 1,
-                       "l2": "inputs (%.0f MB/GPU) larger than L2" % (23 * 8 * n / 1e6),
+                       "l2": "inputs (%.0f MB per GPU) larger than L2 (129 MB)"
+                             % (23 * 8 * n / 1e6),
                        "parallelism": f"{world} independent point shards"},
+            "fp64_gpu": fp64, "accuracy": accuracy,
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
-            "clocks": clk.summary(), "gpu_launches": args.steps,
-            "kernel_ms": {"median": kernel_ms, "min": min(launch_ms), "max": max(launch_ms)},
+            "clocks": clk.summary(), "gpu_launches": launches,
+            "phases_ms": {k: {"ms": v[0], "launches": v[1]} for k, v in phases.items() if v[1]},
             "generator_s": gen_s,
         }
         print(json.dumps(line))

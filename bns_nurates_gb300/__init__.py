@@ -11,9 +11,10 @@ from ._capi import (BREM_BRT06, BREM_GP19, BREM_HR98, FP64, MIXED,  # noqa: F401
 from .api import (BnsnError, ComputeM1Opacities, ComputeM1OpacitiesNotStimulated,  # noqa: F401
                   ComputeSpectralOpacitiesNotStimulatedAbs,
                   ComputeSpectralOpacitiesStimulatedAbs, distr_from_m1, flags_tuple,
-                  fp64_peak_tflops, gauss_legendre, m1_opacities, m1_opacities_host, nu_equilibrium,
-                  opacity_flags, opacity_params, params_tuple, quad_arrays, set_gp19_table,
-                  spectral_opacities, synthetic_points)
+                  fp64_peak_tflops, gauss_legendre, kernel_launches, m1_opacities,
+                  m1_opacities_host, nu_equilibrium, opacity_flags, opacity_params, params_tuple,
+                  phase_times, phase_timing, quad_arrays, set_gp19_table, spectral_opacities,
+                  synthetic_points)
 
 
 def lib():

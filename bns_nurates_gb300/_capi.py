@@ -18,6 +18,8 @@ c_double, c_int, c_bool = ctypes.c_double, ctypes.c_int, ctypes.c_bool
 # status codes
 OK, ERR_ARG, ERR_NQUAD, ERR_CUDA, ERR_NO_TABLE, ERR_NO_DEVICE = range(6)
 FP64, MIXED = 0, 1
+NUM_PHASES = 7
+PHASES = ("prelude", "pair", "brem", "neps", "final", "spectral", "aux")
 BREM_HR98, BREM_BRT06, BREM_GP19 = 0, 1, 2
 
 
@@ -137,6 +139,9 @@ SIGNATURES = {
     "bnsn_synthetic_points": (c_int, [ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64, P, P,
                                       c_int]),
     "bnsn_fp64_peak_probe": (c_int, [ctypes.c_int64, P]),
+    "bnsn_phase_timing": (c_int, [c_int]),
+    "bnsn_phase_times": (c_int, [P, P]),
+    "bnsn_kernel_launches": (ctypes.c_int64, []),
     "bnsn_status_string": (ctypes.c_char_p, [c_int]),
     "bnsn_last_error": (ctypes.c_char_p, []),
     "bnsn_version": (c_int, []),

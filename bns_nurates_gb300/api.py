@@ -230,6 +230,24 @@ def fp64_peak_tflops(iters=1 << 16):
     return v.value
 
 
+def phase_timing(enable):
+    """Bracket every library kernel launch with CUDA events (diagnostic)."""
+    _check(C.load().bnsn_phase_timing(int(bool(enable))))
+
+
+def phase_times():
+    """Per-phase device ms and launch counts since the previous call."""
+    ms = (ctypes.c_double * C.NUM_PHASES)()
+    n = (ctypes.c_int64 * C.NUM_PHASES)()
+    _check(C.load().bnsn_phase_times(ms, n))
+    return {name: (ms[k], n[k]) for k, name in enumerate(C.PHASES)}
+
+
+def kernel_launches():
+    """Kernels launched by the library in this process."""
+    return int(C.load().bnsn_kernel_launches())
+
+
 def m1_opacities_host(eos, m1, flags, params, quad_1d, quad_2d=None, stim_abs=1,
                       precision="fp64", out=None):
     """Grey opacities of host (numpy or pinned torch) arrays, copies included."""

@@ -81,7 +81,9 @@ cudaError_t launch_distr_from_m1(const DistrLaunch& L, cudaStream_t stream, int 
 {
     if (L.npts <= 0)
         return cudaSuccess;
+    phase_mark(kPhAux, 0, stream);
     distr_from_m1_kernel<<<grid_for(L.npts, 128, num_sms), 128, 0, stream>>>(L);
+    phase_mark(kPhAux, 1, stream);
     return cudaGetLastError();
 }
 
@@ -89,7 +91,9 @@ cudaError_t launch_nu_equilibrium(const EquilLaunch& L, cudaStream_t stream, int
 {
     if (L.npts <= 0)
         return cudaSuccess;
+    phase_mark(kPhAux, 0, stream);
     nu_equilibrium_kernel<<<grid_for(L.npts, 128, num_sms), 128, 0, stream>>>(L);
+    phase_mark(kPhAux, 1, stream);
     return cudaGetLastError();
 }
 

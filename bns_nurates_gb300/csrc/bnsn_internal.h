@@ -48,6 +48,23 @@ struct OpacityLaunch
     double* sout[16];      // j, kappa, j_s, kappa_s per species
 };
 
+// Kernel phases of the timing hooks (bnsn_phase_times).
+enum Phase
+{
+    kPhPrelude = 0,
+    kPhPair,
+    kPhBrem,
+    kPhNeps,
+    kPhFinal,
+    kPhSpectral,
+    kPhAux,
+    kNumPhases
+};
+
+// Records a CUDA event on `stream` before (end = 0) or after (end = 1) a
+// launch of `phase` when phase timing is on; always counts launches (end = 1).
+void phase_mark(int phase, int end, cudaStream_t stream);
+
 // Grey opacities in chunks of ws_points points; ws holds ws_points per-point
 // scratch records of grey_point_scratch_bytes() each.
 size_t grey_point_scratch_bytes();

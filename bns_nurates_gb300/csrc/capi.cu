@@ -16,6 +16,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <string>
@@ -260,7 +261,85 @@ int attach_device(OpacityLaunch* L, DeviceState** st)
 
 } // namespace
 
+// ---------------------------------------------------------------------------
+// phase timing and launch counting
+// ---------------------------------------------------------------------------
+namespace {
+
+std::atomic<int64_t> g_launches{0};
+std::atomic<int> g_timing{0};
+std::mutex g_timer_mu;
+std::vector<cudaEvent_t> g_ev_pool;   // events owned by the timer
+std::vector<std::pair<int, size_t>> g_ev_marks; // phase, index of the start event
+size_t g_ev_used = 0;
+
+} // namespace
+
+void bnsn::phase_mark(int phase, int end, cudaStream_t stream)
+{
+    if (end)
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+    if (!g_timing.load(std::memory_order_relaxed))
+        return;
+    std::lock_guard<std::mutex> lk(g_timer_mu);
+    if (g_ev_used == g_ev_pool.size())
+    {
+        cudaEvent_t ev;
+        if (cudaEventCreate(&ev) != cudaSuccess)
+            return;
+        g_ev_pool.push_back(ev);
+    }
+    if (!end)
+        g_ev_marks.push_back({phase, g_ev_used});
+    cudaEventRecord(g_ev_pool[g_ev_used++], stream);
+}
+
 extern "C" {
+
+int bnsn_phase_timing(int enable)
+{
+    g_timing.store(enable ? 1 : 0);
+    return BNSN_OK;
+}
+
+int bnsn_phase_times(double* ms, int64_t* launches)
+{
+    g_err.clear();
+    if (!ms || !launches)
+        return fail(BNSN_ERR_ARG, "ms/launches is NULL");
+    for (int q = 0; q < BNSN_NUM_PHASES; ++q)
+    {
+        ms[q]       = 0.;
+        launches[q] = 0;
+    }
+    std::lock_guard<std::mutex> lk(g_timer_mu);
+    int rc = BNSN_OK;
+    for (const auto& m : g_ev_marks)
+    {
+        if (m.second + 1 >= g_ev_used)
+            break;
+        float t = 0.f;
+        cudaError_t e = cudaEventSynchronize(g_ev_pool[m.second + 1]);
+        if (e == cudaSuccess)
+            e = cudaEventElapsedTime(&t, g_ev_pool[m.second], g_ev_pool[m.second + 1]);
+        if (e != cudaSuccess)
+        {
+            rc = cuda_fail(e, "phase timing");
+            break;
+        }
+        if (m.first >= 0 && m.first < BNSN_NUM_PHASES)
+        {
+            ms[m.first] += t;
+            launches[m.first] += 1;
+        }
+    }
+    g_ev_marks.clear();
+    g_ev_used = 0;
+    return rc;
+}
+
+int64_t bnsn_kernel_launches(void) { return g_launches.load(); }
+
 
 int bnsn_version(void) { return 100; }
 

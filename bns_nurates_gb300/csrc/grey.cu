@@ -776,6 +776,7 @@ cudaError_t launch_brem(const OpacityLaunch& L, int64_t p0, int64_t np, double* 
                         cudaStream_t st, int sms, int add)
 {
     const int64_t wb = (np + kWarps - 1) / kWarps;
+    phase_mark(kPhBrem, 0, st);
     if (L.brem_impl == 0)
         grey_brem_kernel<MIXED, 0>
             <<<grid_for(grey_brem_kernel<MIXED, 0>, kWarps * 32, wb, sms), kWarps * 32, 0, st>>>(
@@ -788,6 +789,7 @@ cudaError_t launch_brem(const OpacityLaunch& L, int64_t p0, int64_t np, double* 
         grey_brem_kernel<MIXED, 2>
             <<<grid_for(grey_brem_kernel<MIXED, 2>, kWarps * 32, wb, sms), kWarps * 32, 0, st>>>(
                 L, p0, np, ws, add);
+    phase_mark(kPhBrem, 1, st);
     return cudaGetLastError();
 }
 
@@ -804,16 +806,20 @@ cudaError_t launch_grey(const OpacityLaunch& L, cudaStream_t st, int sms, double
     {
         const int64_t np = (L.npts - p0) < ws_points ? (L.npts - p0) : ws_points;
         const int64_t wb = (np + kWarps - 1) / kWarps;
+        phase_mark(kPhPrelude, 0, st);
         grey_prelude_kernel<<<grid_for(grey_prelude_kernel, kWarps * 32, wb, sms), kWarps * 32, 0,
                               st>>>(L, p0, np, ws);
+        phase_mark(kPhPrelude, 1, st);
         if (L.use_pair)
         {
+            phase_mark(kPhPair, 0, st);
             if (L.mixed)
                 grey_pair_kernel<true><<<grid_for(grey_pair_kernel<true>, kWarps * 32, wb, sms),
                                          kWarps * 32, 0, st>>>(L, p0, np, ws);
             else
                 grey_pair_kernel<false><<<grid_for(grey_pair_kernel<false>, kWarps * 32, wb, sms),
                                           kWarps * 32, 0, st>>>(L, p0, np, ws);
+            phase_mark(kPhPair, 1, st);
         }
         if (L.use_brem)
         {
@@ -823,10 +829,16 @@ cudaError_t launch_grey(const OpacityLaunch& L, cudaStream_t st, int sms, double
                 return e;
         }
         if (L.use_inel)
+        {
+            phase_mark(kPhNeps, 0, st);
             grey_neps_kernel<<<grid_for(grey_neps_kernel, kWarps * 32, wb, sms), kWarps * 32, 0,
                                st>>>(L, p0, np, ws);
+            phase_mark(kPhNeps, 1, st);
+        }
+        phase_mark(kPhFinal, 0, st);
         grey_final_kernel<<<grid_for(grey_final_kernel, 128, (np + 127) / 128, sms), 128, 0, st>>>(
             L, p0, np, ws);
+        phase_mark(kPhFinal, 1, st);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess)
             return e;

@@ -329,7 +329,9 @@ cudaError_t launch_spectral_fp64(const OpacityLaunch& L, cudaStream_t stream, in
         blocks_per_sm = 1;
     const int64_t need = (L.npts + kWarps - 1) / kWarps;
     const int64_t cap  = (int64_t)num_sms * blocks_per_sm;
+    phase_mark(kPhSpectral, 0, stream);
     spectral_fp64_kernel<<<(int)(need < cap ? need : cap), kWarps * 32, 0, stream>>>(L, G);
+    phase_mark(kPhSpectral, 1, stream);
     return cudaGetLastError();
 }
 

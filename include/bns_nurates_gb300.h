@@ -187,8 +187,15 @@ typedef struct SpectralOpacities
  * Points are independent.  Every per-point quantity is a separate device
  * array of length npts (structure of arrays, one pointer per struct field),
  * so callers can pass their own grid-function storage.  Calls are
- * stream-ordered on `stream` (a cudaStream_t; NULL = default stream), do not
- * synchronise the host, and allocate nothing.
+ * stream-ordered on `stream` (a cudaStream_t; NULL = default stream) and do
+ * not synchronise the host.
+ *
+ * Device memory: bnsn_m1_opacities keeps a per-point scratch record (about
+ * 6 KB) for at most 16384 points at a time.  It takes that scratch from a
+ * library-owned stream-ordered memory pool (one per device, created on the
+ * first call), allocating and freeing it in order on `stream`, so calls on
+ * different streams never share scratch.  The pool keeps its memory for
+ * later calls.  The other batched calls allocate nothing.
  * ====================================================================== */
 
 typedef enum bnsn_status
@@ -362,6 +369,21 @@ int bnsn_synthetic_points(uint64_t seed, int64_t first, int64_t npts,
  * the FP64-pipe roofline of the opacity kernels.  A diagnostic with no
  * counterpart in the reference. */
 int bnsn_fp64_peak_probe(int64_t iters, double* tflops);
+
+/* Per-phase device timing of the library's own kernels (diagnostics with no
+ * counterpart in the reference).  While enabled, every kernel launch is
+ * bracketed by CUDA events on its stream; bnsn_phase_times waits for the
+ * recorded events, adds each launch's duration to ms[phase] and its count to
+ * launches[phase] (arrays of BNSN_NUM_PHASES entries, accumulated since the
+ * previous bnsn_phase_times call), and clears the record.  Phases:
+ * 0 grey prelude, 1 pair cells, 2 brem cells, 3 NES/NPS pairs, 4 grey
+ * assembly, 5 spectral, 6 distribution/equilibrium.  Timing one device at a
+ * time is supported. */
+#define BNSN_NUM_PHASES 7
+int bnsn_phase_timing(int enable);
+int bnsn_phase_times(double* ms, int64_t* launches);
+/* Number of kernels this library has launched in the process. */
+int64_t bnsn_kernel_launches(void);
 
 const char* bnsn_status_string(int status);
 /* Text of the most recent error on the calling thread ("" if none). */
