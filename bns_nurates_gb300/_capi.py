@@ -18,6 +18,7 @@ c_double, c_int, c_bool = ctypes.c_double, ctypes.c_int, ctypes.c_bool
 # status codes
 OK, ERR_ARG, ERR_NQUAD, ERR_CUDA, ERR_NO_TABLE, ERR_NO_DEVICE = range(6)
 FP64, MIXED = 0, 1
+NOALLOC_MAX_POINTS = 4096
 NUM_PHASES = 7
 PHASES = ("prelude", "pair", "brem", "neps", "final", "spectral", "aux")
 BREM_HR98, BREM_BRT06, BREM_GP19 = 0, 1, 2
@@ -127,6 +128,8 @@ class SpectralSoA(ctypes.Structure):
 # every entry point of the header, with its ctypes signature
 SIGNATURES = {
     "bnsn_m1_opacities": (c_int, [P, P, P, P, P, P, P, c_int, c_int, P, ctypes.c_int64, P]),
+    "bnsn_m1_opacities_noalloc": (c_int, [P, P, P, P, P, P, P, c_int, c_int, P, ctypes.c_int64,
+                                          P]),
     "bnsn_spectral_opacities": (c_int, [P, P, P, P, P, P, P, c_int, c_int, c_int, P,
                                         ctypes.c_int64, P]),
     "bnsn_distr_from_m1": (c_int, [P, P, ctypes.c_int64, P]),

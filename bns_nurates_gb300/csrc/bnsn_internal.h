@@ -66,8 +66,15 @@ enum Phase
 void phase_mark(int phase, int end, cudaStream_t stream);
 
 // Grey opacities in chunks of ws_points points; ws holds ws_points per-point
-// scratch records of grey_point_scratch_bytes() each.
+// scratch records of grey_point_scratch_bytes() (= kGreyRecordBytes) each.
+constexpr size_t kGreyRecordBytes = 766 * sizeof(double);
 size_t grey_point_scratch_bytes();
+
+// Static scratch of bnsn_m1_opacities_noalloc: room for kNoAllocPoints grey
+// records in a file-scope __device__ array.  noalloc_scratch() looks up its
+// address on the current device (cudaGetSymbolAddress, cached per device).
+constexpr int64_t kNoAllocPoints = 4096;
+cudaError_t noalloc_scratch(int device, double** ptr);
 cudaError_t launch_grey(const OpacityLaunch& L, cudaStream_t stream, int num_sms, double* ws,
                         int64_t ws_points);
 cudaError_t launch_spectral_fp64(const OpacityLaunch& L, cudaStream_t stream, int num_sms);

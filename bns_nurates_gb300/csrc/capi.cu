@@ -404,6 +404,74 @@ int bnsn_m1_opacities(const MyQuadrature* quad_1d, const MyQuadrature* quad_2d,
     return ef == cudaSuccess ? BNSN_OK : cuda_fail(ef, "grey scratch release");
 }
 
+// Grey opacities with the per-point scratch in a static device array instead
+// of the stream-ordered pool: for callers that must not allocate device memory
+// inside the call (see the header).  Same arguments and results as
+// bnsn_m1_opacities, at most BNSN_NOALLOC_MAX_POINTS points per call.
+int bnsn_m1_opacities_noalloc(const MyQuadrature* quad_1d, const MyQuadrature* quad_2d,
+                              const OpacityFlags* flags, const OpacityParams* params,
+                              const bnsn_eos_soa* eos, const bnsn_m1_soa* m1,
+                              const bnsn_distr_soa* distr, int stim_abs, int precision,
+                              const bnsn_m1_opacities_soa* out, int64_t npts, void* stream)
+{
+    static_assert(BNSN_NOALLOC_MAX_POINTS == kNoAllocPoints, "static scratch capacity");
+    g_err.clear();
+    if (precision != BNSN_FP64 && precision != BNSN_MIXED)
+        return fail(BNSN_ERR_ARG, "unknown precision");
+    if (!out)
+        return fail(BNSN_ERR_ARG, "out is NULL");
+    OpacityLaunch L;
+    memset(&L, 0, sizeof(L));
+    int rc;
+    if ((rc = fill_common(quad_1d, quad_2d, flags, params, stim_abs, &L)))
+        return rc;
+    if ((rc = fill_points(eos, m1, distr, true, npts, &L)))
+        return rc;
+    if (npts > kNoAllocPoints)
+        return fail(BNSN_ERR_ARG, "npts = " + std::to_string(npts) +
+                                      " exceeds BNSN_NOALLOC_MAX_POINTS = 4096, the capacity of "
+                                      "the static scratch: split the batch, or call "
+                                      "bnsn_m1_opacities");
+    double* const* o[5] = {out->eta_0, out->kappa_0_a, out->eta, out->kappa_a, out->kappa_s};
+    for (int q = 0; q < 5; ++q)
+        for (int s = 0; s < 4; ++s)
+        {
+            if (npts > 0 && !o[q][s])
+                return fail(BNSN_ERR_ARG, "an output pointer is NULL");
+            L.out[q * 4 + s] = o[q][s];
+        }
+    L.mixed = precision == BNSN_MIXED;
+    // device checks without the per-device state of the pooled calls (whose
+    // first use creates the memory pool)
+    int dev = 0, ndev = 0, major = 0, minor = 0, sms = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(BNSN_ERR_NO_DEVICE, "no CUDA device");
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess)
+        return cuda_fail(e, "cudaGetDevice");
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+    if (major != 10 || minor != 3)
+        return fail(BNSN_ERR_NO_DEVICE, "device is not sm_103 (GB300)");
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+        return cuda_fail(e, "cudaDeviceGetAttribute");
+    if (L.use_brem && L.brem_impl == BREM_GP19)
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        auto it = g_dev.find(dev);
+        if (it == g_dev.end() || !it->second.gp19)
+            return fail(BNSN_ERR_NO_TABLE, "GP19 brem requested but no table loaded");
+        L.gp19 = it->second.g;
+    }
+    double* ws = nullptr;
+    if ((e = noalloc_scratch(dev, &ws)) != cudaSuccess)
+        return cuda_fail(e, "cudaGetSymbolAddress(static grey scratch)");
+    if (npts == 0)
+        return BNSN_OK;
+    e = launch_grey(L, (cudaStream_t)stream, sms, ws, kNoAllocPoints);
+    return e == cudaSuccess ? BNSN_OK : cuda_fail(e, "grey kernel launch");
+}
+
 int bnsn_spectral_opacities(const MyQuadrature* quad_1d, const OpacityFlags* flags,
                             const OpacityParams* params, const bnsn_eos_soa* eos,
                             const bnsn_m1_soa* m1, const bnsn_distr_soa* distr,

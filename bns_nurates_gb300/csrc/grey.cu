@@ -62,6 +62,7 @@ struct PointTab
     double siso[4];      // iso per species
 };
 static_assert(sizeof(PointTab) % sizeof(double) == 0, "PointTab must be double words");
+static_assert(sizeof(PointTab) == kGreyRecordBytes, "grey record size");
 constexpr int kTabWords = sizeof(PointTab) / sizeof(double);
 
 size_t grey_point_scratch_bytes() { return sizeof(PointTab); }

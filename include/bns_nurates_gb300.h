@@ -282,6 +282,34 @@ int bnsn_m1_opacities(const MyQuadrature* quad_1d, const MyQuadrature* quad_2d,
                       const bnsn_m1_opacities_soa* out, int64_t npts,
                       void* stream);
 
+/* Grey M1 opacities without any device allocation (no counterpart in the
+ * reference).  Same arguments and results as bnsn_m1_opacities, but the
+ * per-point scratch records live in a static device array inside the library
+ * (room for BNSN_NOALLOC_MAX_POINTS points, 24 MiB) instead of the
+ * stream-ordered pool.  It is meant for callers that must not allocate device
+ * memory inside the call: codes whose device memory is owned by their own
+ * allocator (hydro/AMR frameworks that reserve most of HBM at start-up, where
+ * an extra driver allocation can fail or fragment it), and codes that keep
+ * driver allocation calls out of their time step.
+ *   - npts > BNSN_NOALLOC_MAX_POINTS is rejected with BNSN_ERR_ARG (split the
+ *     batch, or call bnsn_m1_opacities).
+ *   - The first call on each device looks up the array's address with that
+ *     device current (cudaGetSymbolAddress, which may load a module); make
+ *     that first call (npts may be 0) before any stream capture.
+ *   - Nothing in the array needs to start at zero: every scratch value a
+ *     kernel reads is written earlier in the same call.
+ *   - There is one array per device: calls that overlap in time on one device
+ *     (different streams or host threads without ordering between them) race
+ *     on it and give wrong results.  Order such calls on one stream or with
+ *     events. */
+#define BNSN_NOALLOC_MAX_POINTS 4096
+int bnsn_m1_opacities_noalloc(const MyQuadrature* quad_1d, const MyQuadrature* quad_2d,
+                              const OpacityFlags* flags, const OpacityParams* params,
+                              const bnsn_eos_soa* eos, const bnsn_m1_soa* m1,
+                              const bnsn_distr_soa* distr, int stim_abs,
+                              int precision, const bnsn_m1_opacities_soa* out,
+                              int64_t npts, void* stream);
+
 /* Spectral opacities of npts points at n_energies neutrino energies
  * (`energies` is a host array, MeV).  Replaces
  * ComputeSpectralOpacitiesStimulatedAbs (stimulated = 1,
