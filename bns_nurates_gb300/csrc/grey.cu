@@ -33,6 +33,7 @@
 
 #include <cuda_runtime.h>
 
+#include "bnsn_df.cuh"
 #include "bnsn_fp32.cuh"
 #include "bnsn_fp64.cuh"
 #include "bnsn_internal.h"
@@ -573,12 +574,244 @@ struct NepsTab
     double same_cf;
 };
 
+// Energies of NES item (r, i, j) (m1_opacities.hpp:880-905).
+__device__ __forceinline__ void neps_energies(int r, double xi, double xj, double tn, double* nu,
+                                              double* nub)
+{
+    if (!r)
+    {
+        *nu  = 0.5 * tn * xi * (1. - xj);
+        *nub = 0.5 * tn * xi * (1. + xj);
+    }
+    else
+    {
+        *nu  = 0.5 * tn * (1. - xj) / xi;
+        *nub = 0.5 * tn * (1. + xj) / xi;
+    }
+}
+
+// The FP64 item sums of one point (the plain path, and the mixed path's
+// fallback for points outside the FP32 range envelope).
+__device__ __forceinline__ void neps_items_fp64(const NepsPoint& NP, const Distr& d, bool same_cf,
+                                                int n2, double tn, bool stim, bool nbb,
+                                                const double* s_x2, const double* s_w2,
+                                                const double* s_wx, const double* s_wx3,
+                                                int lane, double* acc)
+{
+    const int nn2 = n2 * n2;
+    for (int it = lane; it < 2 * nn2; it += 32)
+    {
+        const int r   = it >= nn2;
+        const int rem = it - r * nn2;
+        const int i = rem / n2, j = rem - (rem / n2) * n2;
+        double nu, nub;
+        neps_energies(r, s_x2[i], s_x2[j], tn, &nu, &nub);
+        const double w4 = (nu * nu) * (nub * nub);
+        double g[4], gb[4];
+        total_nu_f4(nu, d, same_cf, g);
+        total_nu_f4(nub, d, same_cf, gb);
+        double em1[4], ab1[4], em2[4], ab2[4];
+        neps_pair(NP, nu, nub, em1, ab1, em2, ab2);
+        const double Wr = (r ? s_wx3[i] : s_wx[i]) * s_w2[j];
+#pragma unroll
+        for (int s = 0; s < 4; ++s)
+        {
+            const double e1 = em1[s] * gb[s];
+            const double a1 = ab1[s] * (nbb ? 1. : 1. - gb[s]);
+            const double e2 = em2[s] * g[s];
+            const double a2 = ab2[s] * (nbb ? 1. : 1. - g[s]);
+            double EM1, AB1, EM2, AB2;
+            if (stim)
+            {
+                AB1 = w4 * g[s] * (e1 + a1);
+                EM1 = w4 * e1;
+                AB2 = w4 * gb[s] * (e2 + a2);
+                EM2 = w4 * e2;
+            }
+            else
+            {
+                AB1 = w4 * g[s] * a1;
+                EM1 = w4 * (1. - g[s]) * e1;
+                AB2 = w4 * gb[s] * a2;
+                EM2 = w4 * (1. - gb[s]) * e2;
+            }
+            acc[s] += Wr * (EM1 + EM2);
+            acc[4 + s] += Wr * (AB1 + AB2);
+            acc[8 + s] += Wr * (nu * EM1 + nub * EM2);
+            acc[12 + s] += Wr * (nu * AB1 + nub * AB2);
+        }
+    }
+}
+
+// Per-point data of the mixed item loop.
+struct NepsMixed
+{
+    dfm::df reta[2][5]; // unreflected F_1..F_5 at eta for e- (0) and e+ (1)
+    dfm::df eta[2];
+    float wt[4], invTt[4], etat[4], wf[4], lbf[4], invTf[4], cf[4];
+};
+
+// TotalNuF (distribution.hpp:298-315) and 1 - TotalNuF in FP32; the blocking
+// factor is formed from the complements of the two parts (w_t + w_f = 1 for
+// the reconstructed distribution), so it keeps its relative precision where
+// the occupation approaches 1.
+__device__ __forceinline__ void total_nu_f32(float omega, const NepsMixed& Q, float* g, float* gm)
+{
+    const float lw = logf(omega);
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+    {
+        const float arg = omega * Q.invTt[s] - Q.etat[s];
+        const float t   = expf(-fabsf(arg));
+        const float inv = 1.f / (t + 1.f);
+        const float ft  = arg > 0.f ? t * inv : inv;
+        const float ftm = arg > 0.f ? inv : t * inv;
+        const float fn  = expf(Q.lbf[s] + Q.cf[s] * lw - omega * Q.invTf[s]);
+        g[s]            = Q.wt[s] * ft + Q.wf[s] * fn;
+        gm[s]           = Q.wt[s] * ftm + Q.wf[s] * (1.f - fn);
+    }
+}
+
+// NEPSExpFunc (functions.hpp:4401-4413) in FP32; expm1 keeps 1 - e^{-|d|}
+// accurate for small |d|.
+__device__ __forceinline__ float neps_exp_f32(float d, bool neg)
+{
+    const float a  = fabsf(d);
+    const float e  = expf(-a);
+    const float dn = -expm1f(-a) + (d == 0.f ? 1.f : 0.f);
+    return (neg ? 1.f : -e) / dn;
+}
+
+// One item of the mixed path: dimensionless kernels r1 = R(nu, nub) / pre,
+// r2 = R(nub, nu) / pre summed over e- and e+ with NEPSExpFunc applied
+// (em1, ab1, em2, ab2 per species).  The Fermi integrals and the
+// Mezzacappa-Bruenn brackets (kernel_nes.hpp:50-132) run in df: they cancel
+// catastrophically.  The branch structure of neps_pair is kept; the Taylor
+// branches near w, w' -> 0 run in FP64.
+__device__ __forceinline__ void neps_item_mixed(const NepsPoint& P, const NepsMixed& Q, double w,
+                                                double wp, float* em1, float* ab1, float* em2,
+                                                float* ab2)
+{
+    using namespace dfm;
+    const double x = (w > wp) ? w : wp;
+    const double y = (w < wp) ? w : wp;
+    const double d1 = wp - w, d2 = w - wp;
+    const bool n1 = signbit(d1) != 0, n2 = signbit(d2) != 0;
+    const float efa = neps_exp_f32((float)d1, n1);
+    const float efb = neps_exp_f32((float)d2, n2);
+    const float sign1 = n1 ? 1.f : -1.f;
+    const float sign2 = n2 ? 1.f : -1.f;
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+        em1[s] = ab1[s] = em2[s] = ab2[s] = 0.f;
+    // w-dependent df building blocks shared by both leptons
+    const df W  = from_double(w), WP = from_double(wp);
+    const df S  = add(W, WP);
+    const df Pp = mul(W, WP);
+    const df Dn = mul(Pp, Pp);
+    const df X  = from_double(x), Y = from_double(y);
+#pragma unroll 1
+    for (int e = 0; e < 2; ++e)
+    {
+        const double eta = e ? P.eta1 : P.eta0;
+        float r1[4], r2[4];
+        if (y > eta * 1e-3)
+        {
+            // F_k(eta - w'), F_k(eta - w) and F_k(eta) - F_k(eta - |w - w'|) as
+            // differences (fdi_diff15): no cancellation of the reflection
+            // polynomials in degenerate matter
+            const df aw = from_double(eta - w), awp = from_double(eta - wp);
+            const double adw = fabs(w - wp);
+            const df aab = from_double(eta - adw);
+            df rw[5], rwp[5], rab[5];
+            fdi_raw15(aw, rw);
+            fdi_raw15(awp, rwp);
+            fdi_raw15(aab, rab);
+            df dw[5], d5[5];
+            fdi_diff15(rw, rwp, aw, awp, from_double(w - wp), dw);
+            fdi_diff15(rab, Q.reta[e], aab, Q.eta[e], from_double(adw), d5);
+            const df dabs[3] = {d5[2], d5[3], d5[4]};
+            // mb_int_out(w, w') = b1 A + b2 B; the (w', w) direction has
+            // dw -> -dw and the other sign (kernel_nes.hpp:50-78)
+            const df T1 = add(dw[3], mul(add(mul(S, dw[2]), mul(mul(Pp, 3.f), dw[1])), 2.f));
+            const df U  = add(mul(X, dabs[1]), mul(mul(mul(X, X), 2.f), dabs[0]));
+            const df V  = add(neg(mul(Y, dabs[1])), mul(mul(mul(Y, Y), 2.f), dabs[0]));
+            const df ST = mul(S, T1);
+            constexpr dfc kFifth(0.2); // 0.2f is not 0.2: the brackets cancel to 1e-6
+            const df d2 = mul(dabs[2], mk(kFifth)), w4 = mul(dw[4], mk(kFifth));
+            const df c1 = sub(mul(d2, sign1), w4);
+            const df c2 = add(mul(d2, sign2), w4);
+            const df s6 = mul(dw[0], 6.f);
+            const df A1 = sub(div(add(sub(c1, ST), mul(U, sign1)), Dn), s6);
+            const df B1 = div(add(c1, mul(V, sign1)), Dn);
+            const df A2 = add(div(add(add(c2, ST), mul(U, sign2)), Dn), s6);
+            const df B2 = div(add(c2, mul(V, sign2)), Dn);
+            // couplings of neps_couplings: species s pairs (b1, b2) from
+            // {B+ or B-, B0} in an order set by the lepton
+            constexpr dfc kBp(k::NepsBPlus), kBm(k::NepsBMinus), kBz(k::NepsBZero);
+            const df Az1 = mul(A1, mk(kBz)), Bz1 = mul(B1, mk(kBz));
+            const df Az2 = mul(A2, mk(kBz)), Bz2 = mul(B2, mk(kBz));
+#pragma unroll
+            for (int s = 0; s < 4; ++s)
+            {
+                const df bo     = (s < 2) ? mk(kBp) : mk(kBm);
+                const bool first = ((s & 1) == 0) != (e == 1); // b1 = bo, b2 = B0
+                r1[s] = first ? add(mul(A1, bo), Bz1).hi : add(Az1, mul(B1, bo)).hi;
+                r2[s] = first ? add(mul(A2, bo), Bz2).hi : add(Az2, mul(B2, bo)).hi;
+            }
+        }
+        else
+        {
+            const double* f0e = e ? P.fe1 : P.fe0;
+            const double fd0  = e ? P.fd01 : P.fd00;
+            if (x > eta * 1e-3)
+            {
+                double fx[3];
+                fdi_orders<0, 2>(eta - x, fx);
+                const double f[5] = {fx[2] - f0e[2], fx[1], f0e[1],
+                                     fx[0] + y * fermi_distr(0., 1., eta - x) / 6.,
+                                     f0e[0] - y * fd0 / 6.};
+#pragma unroll
+                for (int s = 0; s < 4; ++s)
+                {
+                    double b1, b2;
+                    neps_couplings(e, s, &b1, &b2);
+                    r1[s] = (float)mb_int_one(x, y, (int)sign1, b1, b2, f);
+                    r2[s] = (float)mb_int_one(x, y, (int)sign2, b1, b2, f);
+                }
+            }
+            else
+            {
+                const double f[3] = {fd0, f0e[0], f0e[1]};
+#pragma unroll
+                for (int s = 0; s < 4; ++s)
+                {
+                    double b1, b2;
+                    neps_couplings(e, s, &b1, &b2);
+                    r1[s] = (float)mb_int_two(w, wp, x, y, b1, b2, f);
+                    r2[s] = (float)mb_int_two(wp, w, x, y, b1, b2, f);
+                }
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < 4; ++s)
+        {
+            em1[s] += -r1[s] * efb;
+            ab1[s] += r1[s] * efa;
+            em2[s] += -r2[s] * efa;
+            ab2[s] += r2[s] * efb;
+        }
+    }
+}
+
+template <bool MIXED>
 __global__ void __launch_bounds__(kWarps * 32)
     grey_neps_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
                      double* __restrict__ scratch)
 {
     __shared__ double s_x2[kMaxQ], s_w2[kMaxQ], s_wx[kMaxQ], s_wx3[kMaxQ];
     __shared__ NepsTab s_nt[kWarps];
+    __shared__ NepsMixed s_nm[MIXED ? kWarps : 1];
     for (int k = threadIdx.x; k < kMaxQ; k += blockDim.x)
     {
         s_x2[k]  = L.x2[k];
@@ -618,58 +851,100 @@ __global__ void __launch_bounds__(kWarps * 32)
 #pragma unroll
         for (int kk = 0; kk < 16; ++kk)
             acc[kk] = 0.;
-        const int nn2 = n2 * n2;
-        for (int it = lane; it < 2 * nn2; it += 32)
+        // FP32 range envelope of the mixed item loop: the occupation of every
+        // species must stay far above the FP32 normal range at its peak.
+        bool fp32_ok = MIXED;
+        if (MIXED)
         {
-            const int r   = it >= nn2;
-            const int rem = it - r * nn2;
-            const int i = rem / n2, j = rem - (rem / n2) * n2;
-            const double xi = s_x2[i], xj = s_x2[j];
-            double nu, nub;
-            if (!r)
-            {
-                nu  = 0.5 * tn * xi * (1. - xj);
-                nub = 0.5 * tn * xi * (1. + xj);
-            }
-            else
-            {
-                nu  = 0.5 * tn * (1. - xj) / xi;
-                nub = 0.5 * tn * (1. + xj) / xi;
-            }
-            const double w4 = (nu * nu) * (nub * nub);
-            double g[4], gb[4];
-            total_nu_f4(nu, N.d, same_cf, g);
-            total_nu_f4(nub, N.d, same_cf, gb);
-            double em1[4], ab1[4], em2[4], ab2[4];
-            neps_pair(NP, nu, nub, em1, ab1, em2, ab2);
-            const double Wr = (r ? s_wx3[i] : s_wx[i]) * s_w2[j];
 #pragma unroll
             for (int s = 0; s < 4; ++s)
             {
-                const double e1 = em1[s] * gb[s];
-                const double a1 = ab1[s] * (nbb ? 1. : 1. - gb[s]);
-                const double e2 = em2[s] * g[s];
-                const double a2 = ab2[s] * (nbb ? 1. : 1. - g[s]);
-                double EM1, AB1, EM2, AB2;
-                if (L.stim)
-                {
-                    AB1 = w4 * g[s] * (e1 + a1);
-                    EM1 = w4 * e1;
-                    AB2 = w4 * gb[s] * (e2 + a2);
-                    EM2 = w4 * e2;
-                }
-                else
-                {
-                    AB1 = w4 * g[s] * a1;
-                    EM1 = w4 * (1. - g[s]) * e1;
-                    AB2 = w4 * gb[s] * a2;
-                    EM2 = w4 * (1. - gb[s]) * e2;
-                }
-                acc[s] += Wr * (EM1 + EM2);
-                acc[4 + s] += Wr * (AB1 + AB2);
-                acc[8 + s] += Wr * (nu * EM1 + nub * EM2);
-                acc[12 + s] += Wr * (nu * AB1 + nub * AB2);
+                const Distr& d = N.d;
+                fp32_ok = fp32_ok && (d.w_t[s] == 0. || d.eta_t[s] > -60.) &&
+                          (d.w_f[s] == 0. || d.beta_f[s] > 1e-30) && (d.temp_t[s] > 0.) &&
+                          (d.temp_f[s] > 0.) && isfinite(d.eta_t[s]) && isfinite(d.beta_f[s]);
             }
+            fp32_ok = fp32_ok && isfinite(NP.eta0);
+        }
+        if (!fp32_ok)
+            neps_items_fp64(NP, N.d, same_cf, n2, tn, L.stim != 0, nbb, s_x2, s_w2, s_wx, s_wx3,
+                            lane, acc);
+        else
+        {
+            NepsMixed& Q = s_nm[MIXED ? (threadIdx.x >> 5) : 0];
+            if (lane < 2)
+            {
+                Q.eta[lane] = dfm::from_double(lane ? NP.eta1 : NP.eta0);
+                dfm::fdi_raw15(Q.eta[lane], Q.reta[lane]);
+            }
+            else if (lane >= 8 && lane < 12)
+            {
+                const int s = lane - 8;
+                const Distr& d = N.d;
+                Q.wt[s]    = (float)d.w_t[s];
+                Q.invTt[s] = (float)(1. / d.temp_t[s]);
+                Q.etat[s]  = (float)d.eta_t[s];
+                Q.wf[s]    = (float)d.w_f[s];
+                Q.lbf[s]   = d.beta_f[s] > 0. ? (float)log(d.beta_f[s]) : -INFINITY;
+                Q.invTf[s] = (float)(1. / d.temp_f[s]);
+                Q.cf[s]    = (float)d.c_f[s];
+            }
+            __syncwarp();
+            const double invT = 1. / T;
+            dfm::df dacc[16];
+#pragma unroll
+            for (int kk = 0; kk < 16; ++kk)
+                dacc[kk] = {0.f, 0.f};
+            const int nn2 = n2 * n2;
+            for (int it = lane; it < 2 * nn2; it += 32)
+            {
+                const int r   = it >= nn2;
+                const int rem = it - r * nn2;
+                const int i = rem / n2, j = rem - (rem / n2) * n2;
+                double nu, nub;
+                neps_energies(r, s_x2[i], s_x2[j], tn, &nu, &nub);
+                const double w = nu * invT, wp = nub * invT;
+                float em1[4], ab1[4], em2[4], ab2[4];
+                neps_item_mixed(NP, Q, w, wp, em1, ab1, em2, ab2);
+                float g[4], gm[4], gb[4], gbm[4];
+                total_nu_f32((float)nu, Q, g, gm);
+                total_nu_f32((float)nub, Q, gb, gbm);
+                const float fw = (float)w, fwp = (float)wp;
+                const float w4 = (fw * fwp) * (fw * fwp);
+                const float Wr = (float)((r ? s_wx3[i] : s_wx[i]) * s_w2[j]);
+#pragma unroll
+                for (int s = 0; s < 4; ++s)
+                {
+                    const float e1 = em1[s] * gb[s];
+                    const float a1 = ab1[s] * (nbb ? 1.f : gbm[s]);
+                    const float e2 = em2[s] * g[s];
+                    const float a2 = ab2[s] * (nbb ? 1.f : gm[s]);
+                    float EM1, AB1, EM2, AB2;
+                    if (L.stim)
+                    {
+                        AB1 = w4 * g[s] * (e1 + a1);
+                        EM1 = w4 * e1;
+                        AB2 = w4 * gb[s] * (e2 + a2);
+                        EM2 = w4 * e2;
+                    }
+                    else
+                    {
+                        AB1 = w4 * g[s] * a1;
+                        EM1 = w4 * gm[s] * e1;
+                        AB2 = w4 * gb[s] * a2;
+                        EM2 = w4 * gbm[s] * e2;
+                    }
+                    dacc[s]      = dfm::add(dacc[s], Wr * (EM1 + EM2));
+                    dacc[4 + s]  = dfm::add(dacc[4 + s], Wr * (AB1 + AB2));
+                    dacc[8 + s]  = dfm::add(dacc[8 + s], Wr * (fw * EM1 + fwp * EM2));
+                    dacc[12 + s] = dfm::add(dacc[12 + s], Wr * (fw * AB1 + fwp * AB2));
+                }
+            }
+            // back to the FP64 layout: sums x pre T^4 (x T for the energy moments)
+            const double T4 = (T * T) * (T * T);
+#pragma unroll
+            for (int kk = 0; kk < 16; ++kk)
+                acc[kk] = dfm::to_double(dacc[kk]) * NP.pre * T4 * (kk >= 8 ? T : 1.);
         }
 #pragma unroll
         for (int kk = 0; kk < 16; ++kk)
@@ -832,8 +1107,12 @@ cudaError_t launch_grey(const OpacityLaunch& L, cudaStream_t st, int sms, double
         if (L.use_inel)
         {
             phase_mark(kPhNeps, 0, st);
-            grey_neps_kernel<<<grid_for(grey_neps_kernel, kWarps * 32, wb, sms), kWarps * 32, 0,
-                               st>>>(L, p0, np, ws);
+            if (L.mixed)
+                grey_neps_kernel<true><<<grid_for(grey_neps_kernel<true>, kWarps * 32, wb, sms),
+                                         kWarps * 32, 0, st>>>(L, p0, np, ws);
+            else
+                grey_neps_kernel<false><<<grid_for(grey_neps_kernel<false>, kWarps * 32, wb, sms),
+                                          kWarps * 32, 0, st>>>(L, p0, np, ws);
             phase_mark(kPhNeps, 1, st);
         }
         phase_mark(kPhFinal, 0, st);
