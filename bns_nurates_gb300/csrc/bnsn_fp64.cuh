@@ -948,6 +948,170 @@ BNSN_DI double gp19_high_t(const Gp19Table& G, double nb, double ye, double T, d
     return k::BremConst * nbnm * S;
 }
 
+// ---------------------------------------------------------------------------
+// GP19 per point: for fixed (nb, Ye, T) the multilinear interpolation of
+// kernel_brem_GP19.hpp:75-139 is linear in the table's w column, so a point
+// needs at most two 1-D profiles over the w axis (computed once) and every
+// (w, w') cell only brackets log w.  The regimes follow BremKernelAbsGP19
+// (kernel_brem_GP19.hpp:357-481):
+//   0 in range; 1 nb < nb_min (scaled by (nb/nb_min)^2); 2 nb < nb_min and
+//   T < T_min; 3 nb < nb_min and T > T_max; 4 T < T_min; 5 T > T_max.
+// Profiles: regimes 0, 1 use p0 at (nb', Ye', T); 2, 4 use p0 at T = 2 and
+// p1 at T = 4; 3, 5 use p0 at T = 48 and p1 at T = 50 (nb' = nb_min for 1-3).
+// ---------------------------------------------------------------------------
+constexpr int kGp19MaxW = 64; // w-axis length handled with profiles
+
+struct Gp19Point
+{
+    int regime;
+    double C;     // BremConst * nb' * 1e18 (x (nb/nb_min)^2 in regimes 1, 2)
+    double nbnm;  // nb' * 1e18 of the high-T extrapolation
+    double r2;    // (nb/nb_min)^2 of regime 3
+    double T;
+    double pT[2]; // temperatures of the two profiles
+    double nbp;   // nb' of the profiles [fm^-3]
+    double yep;   // Ye' of the profiles
+};
+
+BNSN_DI void gp19_point(const Gp19Table& G, double nb_nm, double ye_in, double T, Gp19Point* P)
+{
+    double ye = ye_in, nb = nb_nm * 1e-18;
+    const double nbmax = G.nb[G.d0 - 1], nbmin = G.nb[0];
+    const double yemax = G.ye[G.d1 - 1];
+    const double Tmax = G.t[G.d2 - 1], Tmin = G.t[0];
+    if (ye > yemax)
+        ye = yemax;
+    if (nb > nbmax)
+        nb = nbmax;
+    P->T    = T;
+    P->yep  = ye;
+    P->r2   = 1.;
+    P->pT[0] = P->pT[1] = T;
+    if (nb < nbmin)
+    {
+        const double r = nb / nbmin;
+        P->nbp  = nbmin;
+        P->nbnm = nbmin * 1e+18;
+        if (T < Tmin)
+        {
+            P->regime = 2;
+            P->pT[0]  = 2.0;
+            P->pT[1]  = 4.0;
+            P->C      = k::BremConst * (nbmin * 1e+18) * (r * r);
+        }
+        else if (T > Tmax)
+        {
+            P->regime = 3;
+            P->pT[0]  = 48.0;
+            P->pT[1]  = 50.0;
+            P->C      = k::BremConst * (nbmin * 1e+18);
+            P->r2     = r * r;
+        }
+        else
+        {
+            P->regime = 1;
+            P->C      = k::BremConst * (nbmin * 1e+18) * (r * r);
+        }
+    }
+    else
+    {
+        P->nbp  = nb;
+        P->nbnm = nb * 1e+18;
+        P->C    = k::BremConst * (nb * 1e+18);
+        if (T < Tmin)
+        {
+            P->regime = 4;
+            P->pT[0]  = 2.0;
+            P->pT[1]  = 4.0;
+        }
+        else if (T > Tmax)
+        {
+            P->regime = 5;
+            P->pT[0]  = 48.0;
+            P->pT[1]  = 50.0;
+        }
+        else
+            P->regime = 0;
+    }
+}
+
+// Profile entry at w column l for the (nb', Ye', T') of a point; NaN where
+// the reference's interpolation brackets fail.
+BNSN_DI double gp19_profile_at(const Gp19Table& G, double nbp, double yep, double Tp, int l)
+{
+    double tx, ty, tz;
+    const int i  = gp19_bracket(log(nbp), G.lognb, G.d0, &tx);
+    const int j  = gp19_bracket(yep, G.ye, G.d1, &ty);
+    const int kk = gp19_bracket(Tp, G.t, G.d2, &tz);
+    if (i < 0 || j < 0 || kk < 0)
+        return __longlong_as_double(0x7ff8000000000000LL);
+    const double* g = G.data;
+    const int D1 = G.d1, D2 = G.d2, D3 = G.d3;
+    auto at = [&](int a, int b, int c) {
+        return __ldg(&g[(((int64_t)(a) * D1 + b) * D2 + c) * D3 + l]);
+    };
+    const double a0 = 1. - tx, a1 = tx, b0 = 1. - ty, b1 = ty, c0 = 1. - tz, c1 = tz;
+    return at(i, j, kk) * a0 * b0 * c0 + at(i, j, kk + 1) * a0 * b0 * c1 +
+           at(i, j + 1, kk) * a0 * b1 * c0 + at(i, j + 1, kk + 1) * a0 * b1 * c1 +
+           at(i + 1, j, kk) * a1 * b0 * c0 + at(i + 1, j, kk + 1) * a1 * b0 * c1 +
+           at(i + 1, j + 1, kk) * a1 * b1 * c0 + at(i + 1, j + 1, kk + 1) * a1 * b1 * c1;
+}
+
+// The high-temperature extrapolation (kernel_brem_GP19.hpp:285-355) from the
+// in-range kernels at T = 48 and 50 MeV.
+BNSN_DI double gp19_high_t_from(double R48, double R50, double nbnm, double T, double w)
+{
+    const double nbnm2 = nbnm * nbnm;
+    const double w2    = w * w;
+    const double s50   = 7.0710678118654755;
+    const double K     = 4. * k::BremConst * nbnm2;
+    const double A     = 1. / R50;
+    const double B     = 1. / (K * s50);
+    const double m     = (R50 - R48) / (50.0 - 48.0);
+    const double beta  = 8. * w2 * K * (B * B) / (2. * m * (A * A) * s50 + A * K * B);
+    const double gamma = ((A * beta) - (4. * B * w2)) / (B * nbnm2 * 50.0);
+    const double inv   = 1. / ((w / T) * (w / T) + (nbnm2 / (4. * T)) * gamma);
+    const double S     = (beta * nbnm) / (T * sqrt(T)) * inv;
+    return k::BremConst * nbnm * S;
+}
+
+// One cell from the profiles: v0, v1 are the profile values interpolated at
+// the clipped w; w0 = omega + omega' unclipped.
+BNSN_DI void gp19_cell(const Gp19Point& P, double v0, double v1, double w, double w0,
+                       double* em, double* ab)
+{
+    double s;
+    switch (P.regime)
+    {
+    case 0:
+    case 1: s = P.C * v0; break;
+    case 2:
+    {
+        const double eps = 1e-30;
+        double k2 = P.C * v0, k4 = P.C * v1;
+        k2 = (k2 < eps) ? eps : k2;
+        k4 = (k4 < eps) ? eps : k4;
+        const double m = log(k4 / k2) * 1.4426950408889634;
+        s = k2 * pow(P.T * 0.5, m);
+        s = (s < eps) ? eps : s;
+        break;
+    }
+    case 4:
+    {
+        const double k2 = P.C * v0, k4 = P.C * v1;
+        const double m  = log(k4 / k2) * 1.4426950408889634;
+        s = k2 * pow(P.T * 0.5, m);
+        break;
+    }
+    default: // 3, 5
+        s = gp19_high_t_from(P.C * v0, P.C * v1, P.nbnm, P.T, w) * P.r2;
+        break;
+    }
+    s   = fabs(3. * s);
+    *ab = s;
+    *em = s * safe_exp(-w0 / P.T);
+}
+
 // kernel_brem_GP19.hpp:357-481
 BNSN_DI void gp19_kernel(const Gp19Table& G, double nb_nm, double ye_in, double T,
                          double omega, double omega_p, double* em, double* ab)

@@ -39,6 +39,7 @@ struct OpacityLaunch
     double A2[kMaxM];      // 2-D energy weights (x t): x_i w_i or w_i / x_i^3
     double wx[kMaxQ];      // NES: w_i x_i
     double wx3[kMaxQ];     // NES: w_i / x_i^3
+    double lx2[kMaxQ], l1m[kMaxQ], l1p[kMaxQ]; // NES: log x_i, log(1 - x_i), log(1 + x_i)
     uint32_t cells[kMaxCells]; // a | b << 16, a <= b
     Gp19Dev gp19;
     // spectral launches only

@@ -183,6 +183,9 @@ int fill_common(const MyQuadrature* q1, const MyQuadrature* q2, const OpacityFla
         const double x = L->x2[i], w = L->w2[i];
         L->wx[i]  = w * x;
         L->wx3[i] = w / (x * x * x);
+        L->lx2[i] = log(x);
+        L->l1m[i] = log1p(-x);
+        L->l1p[i] = log1p(x);
     }
     // unordered energy pairs (a <= b), ordered by the sum of the energy
     // factors so that neighbouring lanes see similar Fermi-integral arguments

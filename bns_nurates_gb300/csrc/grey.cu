@@ -386,29 +386,127 @@ __device__ __forceinline__ void load_cell_tab(CellTab& C, const PointTab* __rest
     }
 }
 
+// Mixed-path cell tables (FP32): g and 1 - g per species (1 - g formed in
+// FP64), and nu/T as a double-float pair for the detailed-balance exponent.
+struct CellTab32
+{
+    float g[kMaxM][4];
+    float gm[kMaxM][4];
+    float yh[kMaxM], yl[kMaxM];
+};
+
+// FP32 cell sums: per-lane partial sums of up to 4 cells are flushed into the
+// FP64 accumulators, which bounds the FP32 summation error by a few ulp.
+struct Acc32
+{
+    float v[16];
+    float mag[8]; // sum of |term| of the number moments (em, ab per species)
+    __device__ __forceinline__ void clear()
+    {
+#pragma unroll
+        for (int k = 0; k < 16; ++k)
+            v[k] = 0.f;
+    }
+};
+
+// Largest cancellation factor sum|t| / |sum t| of the number moments of a
+// point (warp-reduced; 1 when every term has one sign).
+__device__ __forceinline__ double cancel_factor(const double* acc, const float* mag)
+{
+    double amp = 1.;
+#pragma unroll
+    for (int s = 0; s < 8; ++s)
+    {
+        const double m   = warp_sum((double)mag[s]);
+        const double tot = fabs(warp_sum(acc[s]));
+        amp = fmax(amp, m > 0. ? m / tot : 1.);
+    }
+    return amp;
+}
+
+// Mixed sums whose terms cancel by more than this are recomputed in FP64: the
+// FP32 rounding of each term (a few 1e-7) must stay below 1e-6 in the result.
+constexpr double kMaxCancel = 2.0;
+
+// add_cell in FP32 for a species-independent kernel (brem): K_em, K_ab are
+// dimensionless, w4 = (y_a y_b)^2; the caller scales by T^4 and the kernel's
+// prefactor.
+template <bool STIM>
+__device__ __forceinline__ void add_cell32(Acc32& A, float Kem, float Kab, const float* ga,
+                                           const float* gma, const float* gb, const float* gmb,
+                                           bool nb_block, float w4, float W1, float W2)
+{
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+    {
+        const int ps   = s ^ 1;
+        const float em = Kem * (nb_block ? 1.f : gmb[ps]);
+        const float am = Kab * gb[ps];
+        float EM, AB;
+        if (STIM)
+        {
+            AB = w4 * ga[s] * (em + am);
+            EM = em * w4;
+        }
+        else
+        {
+            AB = am * (w4 * ga[s]);
+            EM = em * (w4 * gma[s]);
+        }
+        A.v[s] += EM * W1;
+        A.v[4 + s] += AB * W1;
+        A.v[8 + s] += EM * W2;
+        A.v[12 + s] += AB * W2;
+        A.mag[s] += fabsf(EM * W1);
+        A.mag[4 + s] += fabsf(AB * W1);
+    }
+}
+
+// FP32 tables of one point from the FP64 ones.
+__device__ __forceinline__ void fill_tab32(CellTab32& D, const CellTab& C, int M, int lane)
+{
+    for (int e = lane; e < 4 * M; e += 32)
+    {
+        const double gv     = C.g[e >> 2][e & 3];
+        D.g[e >> 2][e & 3]  = (float)gv;
+        D.gm[e >> 2][e & 3] = (float)(1. - gv);
+    }
+    for (int a = lane; a < M; a += 32)
+    {
+        const dfm::df yd = dfm::from_double(C.y[a]);
+        D.yh[a]          = yd.hi;
+        D.yl[a]          = yd.lo;
+    }
+}
+
 template <bool MIXED>
 __global__ void __launch_bounds__(kWarps * 32)
     grey_pair_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
                      double* __restrict__ scratch)
 {
     __shared__ double s_A1[kMaxM], s_A2[kMaxM];
+    __shared__ float s_A1f[kMaxM], s_A2f[kMaxM];
     __shared__ uint32_t s_cells[kMaxCells];
     __shared__ CellTab s_ct[kWarps];
+    __shared__ CellTab32 s_c32[MIXED ? kWarps : 1];
     for (int k = threadIdx.x; k < kMaxM; k += blockDim.x)
     {
-        s_A1[k] = L.A1[k];
-        s_A2[k] = L.A2[k];
+        s_A1[k]  = L.A1[k];
+        s_A2[k]  = L.A2[k];
+        s_A1f[k] = (float)L.A1[k];
+        s_A2f[k] = (float)L.A2[k];
     }
     for (int k = threadIdx.x; k < L.ncell; k += blockDim.x)
         s_cells[k] = L.cells[k];
     __syncthreads();
     const int lane = threadIdx.x & 31;
-    CellTab& C     = s_ct[threadIdx.x >> 5];
+    const int wid  = threadIdx.x >> 5;
+    CellTab& C     = s_ct[wid];
     const int M    = 2 * L.n2;
     const bool nbb = L.neglect_blocking != 0;
     const int64_t nwarp = (int64_t)gridDim.x * kWarps;
 
-    for (int64_t q = (int64_t)blockIdx.x * kWarps + (threadIdx.x >> 5); q < np; q += nwarp)
+    for (int64_t q = (int64_t)blockIdx.x * kWarps + wid; q < np; q += nwarp)
     {
         const int64_t p  = p0 + q;
         PointTab* P      = (PointTab*)(scratch + q * kTabWords);
@@ -427,6 +525,8 @@ __global__ void __launch_bounds__(kWarps * 32)
             const int a = ab & 0xffffu, b = ab >> 16;
             const double nua = C.nu[a], nub = C.nu[b];
             double pe[4], pa[4];
+            // the pair kernel goes negative in some cells (truncated Legendre
+            // expansion), so its weighted sums stay FP64 in both paths
             if (MIXED)
                 pair_kernel_one_exp(T, eta, C.y[a], C.y[b], C.fm[a], C.fp[a], C.fm[b], C.fp[b],
                                     C.f3e, C.f4e, pe, pa);
@@ -463,6 +563,31 @@ __global__ void __launch_bounds__(kWarps * 32)
     }
 }
 
+// Per-warp GP19 state of the brem kernel.
+struct Gp19Warp
+{
+    Gp19Point pt;
+    double p[2][kGp19MaxW];
+    float pf[2][kGp19MaxW];
+};
+
+// Bracket of lw on a log-w axis of d3 entries (binary search, first interval).
+template <class R>
+__device__ __forceinline__ int bracket_sorted(R lw, const R* ax, int d3, R* t)
+{
+    int lo = 0, hi = d3 - 2;
+    while (lo < hi)
+    {
+        const int mid = (lo + hi) >> 1;
+        if (lw <= ax[mid + 1])
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    *t = (lw - ax[lo]) / (ax[lo + 1] - ax[lo]);
+    return lo;
+}
+
 // IMPL: 0 HR98, 1 BRT06, 2 GP19.  ADD: accumulate onto the pair sums.
 template <bool MIXED, int IMPL>
 __global__ void __launch_bounds__(kWarps * 32)
@@ -470,25 +595,41 @@ __global__ void __launch_bounds__(kWarps * 32)
                      double* __restrict__ scratch, int add)
 {
     __shared__ double s_A1[kMaxM], s_A2[kMaxM];
+    __shared__ float s_A1f[kMaxM], s_A2f[kMaxM];
     __shared__ uint32_t s_cells[kMaxCells];
     __shared__ CellTab s_ct[kWarps];
+    __shared__ CellTab32 s_c32[MIXED ? kWarps : 1];
+    __shared__ Gp19Warp s_gw[IMPL == 2 ? kWarps : 1];
+    __shared__ double s_lw[IMPL == 2 ? kGp19MaxW : 1];
+    __shared__ float s_lwf[IMPL == 2 ? kGp19MaxW : 1];
+    const Gp19Table G19 = {L.gp19.d0, L.gp19.d1, L.gp19.d2,    L.gp19.d3,   L.gp19.nb,  L.gp19.ye,
+                           L.gp19.t,  L.gp19.w,  L.gp19.lognb, L.gp19.logw, L.gp19.data};
+    const bool prof = IMPL == 2 && G19.d3 <= kGp19MaxW;
     for (int k = threadIdx.x; k < kMaxM; k += blockDim.x)
     {
-        s_A1[k] = L.A1[k];
-        s_A2[k] = L.A2[k];
+        s_A1[k]  = L.A1[k];
+        s_A2[k]  = L.A2[k];
+        s_A1f[k] = (float)L.A1[k];
+        s_A2f[k] = (float)L.A2[k];
     }
     for (int k = threadIdx.x; k < L.ncell; k += blockDim.x)
         s_cells[k] = L.cells[k];
+    if (IMPL == 2 && prof)
+        for (int k = threadIdx.x; k < G19.d3; k += blockDim.x)
+        {
+            s_lw[k]  = G19.logw[k];
+            s_lwf[k] = (float)G19.logw[k];
+        }
     __syncthreads();
     const int lane = threadIdx.x & 31;
-    CellTab& C     = s_ct[threadIdx.x >> 5];
+    const int wid  = threadIdx.x >> 5;
+    CellTab& C     = s_ct[wid];
     const int M    = 2 * L.n2;
     const bool nbb = L.neglect_blocking != 0;
     const int64_t nwarp = (int64_t)gridDim.x * kWarps;
-    const Gp19Table G19 = {L.gp19.d0, L.gp19.d1, L.gp19.d2,    L.gp19.d3,   L.gp19.nb,  L.gp19.ye,
-                           L.gp19.t,  L.gp19.w,  L.gp19.lognb, L.gp19.logw, L.gp19.data};
+    const double wmin = IMPL == 2 ? G19.w[0] : 0., wmax = IMPL == 2 ? G19.w[G19.d3 - 1] : 0.;
 
-    for (int64_t q = (int64_t)blockIdx.x * kWarps + (threadIdx.x >> 5); q < np; q += nwarp)
+    for (int64_t q = (int64_t)blockIdx.x * kWarps + wid; q < np; q += nwarp)
     {
         const int64_t p = p0 + q;
         PointTab* P     = (PointTab*)(scratch + q * kTabWords);
@@ -496,59 +637,188 @@ __global__ void __launch_bounds__(kWarps * 32)
         __syncwarp();
         load_cell_tab(C, P, M, false, lane);
         if (IMPL == 0)
-        {
             warp_copy((double*)&C.hr, (const double*)&P->hr, sizeof(Hr98Point) / sizeof(double),
                       lane);
-            __syncwarp();
-            if (MIXED && lane == 0)
-                fp32::hr98_mixed_from(C.hr, &C.hm);
-        }
         __syncwarp();
+        if (IMPL == 0 && MIXED && lane == 0)
+            fp32::hr98_mixed_from(C.hr, &C.hm);
+        const double nbp = L.eos[0][p], yep = L.eos[2][p];
+        Gp19Warp& GW     = s_gw[IMPL == 2 ? wid : 0];
+        if (IMPL == 2 && prof)
+        {
+            if (lane == 0)
+                gp19_point(G19, nbp, yep, T, &GW.pt);
+            __syncwarp();
+            const int np19 = (GW.pt.regime >= 2) ? 2 : 1;
+            for (int e = lane; e < np19 * G19.d3; e += 32)
+            {
+                const int pr = e / G19.d3, l = e - pr * G19.d3;
+                const double v = gp19_profile_at(G19, GW.pt.nbp, GW.pt.yep, GW.pt.pT[pr], l);
+                GW.p[pr][l]  = v;
+                GW.pf[pr][l] = (float)v;
+            }
+        }
+        // Mixed cells in FP32 except BRT06, the GP19 high-T extrapolation and
+        // points whose pair sums are negative somewhere: there the outputs
+        // (pair + brem + ...) cancel and would magnify FP32 rounding.
+        bool pair_pos = true;
+        if (MIXED && add)
+        {
+            const double v = lane < 16 ? P->s2d[lane] : 0.;
+            pair_pos = __all_sync(0xffffffffu, !(v < 0.));
+        }
+        const bool fp32_cells =
+            MIXED && pair_pos &&
+            (IMPL == 0 || (IMPL == 2 && prof && GW.pt.regime != 3 && GW.pt.regime != 5));
         double acc[16];
 #pragma unroll
         for (int kk = 0; kk < 16; ++kk)
             acc[kk] = 0.;
-        const double nbp = L.eos[0][p], yep = L.eos[2][p];
-        for (int c = lane; c < L.ncell; c += 32)
+        bool redo = false;
+        if (fp32_cells)
         {
-            const uint32_t ab = s_cells[c];
-            const int a = ab & 0xffffu, b = ab >> 16;
-            const double nua = C.nu[a], nub = C.nu[b];
-            double be, ba;
+            CellTab32& D = s_c32[MIXED ? wid : 0];
+            fill_tab32(D, C, M, lane);
+            __syncwarp();
+            double scale = (T * T) * (T * T);
+            float thr = 0.f, lt2 = 0.f;
             if (IMPL == 0)
+                scale *= C.hm.outer;
+            else
             {
-                if (MIXED)
+                scale *= 3. * GW.pt.C;
+                thr = (float)(1e-30 / GW.pt.C);
+                lt2 = (float)log2(T * 0.5);
+            }
+            Acc32 A;
+            A.clear();
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk)
+                A.mag[kk] = 0.f;
+            int pending = 0;
+            for (int c = lane; c < L.ncell; c += 32)
+            {
+                const uint32_t ab = s_cells[c];
+                const int a = ab & 0xffffu, b = ab >> 16;
+                // x = (nu_a + nu_b) / T as hi + lo (accurate exponent)
+                const dfm::df xs = dfm::add(dfm::df{D.yh[a], D.yl[a]}, dfm::df{D.yh[b], D.yl[b]});
+                const float ex = expf(-xs.hi) * (1.f - xs.lo);
+                float Kab;
+                bool slow = false;
+                if (IMPL == 0)
+                    Kab = fp32::hr98_shape(C.hm, xs.hi);
+                else
                 {
-                    const double x   = (nua + nub) / T;
-                    const float xf   = (float)x;
-                    const float xlo  = (float)(x - (double)xf);
-                    const double sab = C.hm.outer * (double)fp32::hr98_shape(C.hm, xf);
-                    ba = sab;
-                    // e^{-x} = e^{-xf} (1 - xlo): keeps the argument's FP64 bits
-                    be = sab * (double)(expf(-xf) * (1.f - xlo));
+                    float wv = (float)(C.nu[a] + C.nu[b]);
+                    wv       = fminf(fmaxf(wv, (float)wmin), (float)wmax);
+                    float tw;
+                    const int l = bracket_sorted<float>(logf(wv), s_lwf, G19.d3, &tw);
+                    const float v0 = GW.pf[0][l] + tw * (GW.pf[0][l + 1] - GW.pf[0][l]);
+                    if (GW.pt.regime <= 1)
+                        Kab = v0;
+                    else
+                    {
+                        const float v1 = GW.pf[1][l] + tw * (GW.pf[1][l + 1] - GW.pf[1][l]);
+                        Kab = v0 * exp2f(log2f(v1 / v0) * lt2);
+                        // regime 2 clips k2, k4 and s at 1e-30 (rare: exact FP64 cell)
+                        slow = GW.pt.regime == 2 && (v0 < thr || v1 < thr || Kab < thr);
+                    }
+                    Kab = fabsf(Kab);
+                }
+                float Kem = Kab * ex;
+                if (IMPL == 2 && slow)
+                {
+                    const double nua = C.nu[a], nub = C.nu[b];
+                    double w = nua + nub;
+                    w        = w > wmax ? wmax : (w < wmin ? wmin : w);
+                    double tw;
+                    const int l = bracket_sorted<double>(log(w), s_lw, G19.d3, &tw);
+                    const double v0 = GW.p[0][l] * (1. - tw) + GW.p[0][l + 1] * tw;
+                    const double v1 = GW.p[1][l] * (1. - tw) + GW.p[1][l + 1] * tw;
+                    double em, abv;
+                    gp19_cell(GW.pt, v0, v1, w, nua + nub, &em, &abv);
+                    Kab = (float)(abv / (3. * GW.pt.C));
+                    Kem = (float)(em / (3. * GW.pt.C));
+                }
+                const float ya = D.yh[a], yb = D.yh[b];
+                const float w4 = (ya * ya) * (yb * yb);
+                const float W1 = s_A1f[a] * s_A1f[b];
+                if (L.stim)
+                    add_cell32<true>(A, Kem, Kab, D.g[a], D.gm[a], D.g[b], D.gm[b], nbb, w4, W1,
+                                     s_A2f[a] * s_A1f[b]);
+                else
+                    add_cell32<false>(A, Kem, Kab, D.g[a], D.gm[a], D.g[b], D.gm[b], nbb, w4, W1,
+                                      s_A2f[a] * s_A1f[b]);
+                if (a != b)
+                {
+                    if (L.stim)
+                        add_cell32<true>(A, Kem, Kab, D.g[b], D.gm[b], D.g[a], D.gm[a], nbb, w4,
+                                         W1, s_A2f[b] * s_A1f[a]);
+                    else
+                        add_cell32<false>(A, Kem, Kab, D.g[b], D.gm[b], D.g[a], D.gm[a], nbb, w4,
+                                          W1, s_A2f[b] * s_A1f[a]);
+                }
+                if (++pending == 4)
+                {
+#pragma unroll
+                    for (int kk = 0; kk < 16; ++kk)
+                        acc[kk] += (double)A.v[kk];
+                    A.clear();
+                    pending = 0;
+                }
+            }
+#pragma unroll
+            for (int kk = 0; kk < 16; ++kk)
+                acc[kk] = acc[kk] + (double)A.v[kk];
+            // cells of both signs (occupation above 1 makes 1 - g negative):
+            // recompute this point in FP64
+            redo = cancel_factor(acc, A.mag) > kMaxCancel;
+#pragma unroll
+            for (int kk = 0; kk < 16; ++kk)
+                acc[kk] = redo ? 0. : acc[kk] * scale;
+        }
+        if (!fp32_cells || redo)
+        {
+            for (int c = lane; c < L.ncell; c += 32)
+            {
+                const uint32_t ab = s_cells[c];
+                const int a = ab & 0xffffu, b = ab >> 16;
+                const double nua = C.nu[a], nub = C.nu[b];
+                double be, ba;
+                if (IMPL == 0)
+                    hr98_kernel(C.hr, nua, nub, &be, &ba);
+                else if (IMPL == 1)
+                    brt06_kernel(C.brt06_pre, T, nua, nub, &be, &ba);
+                else if (prof)
+                {
+                    double w = nua + nub;
+                    w        = w > wmax ? wmax : (w < wmin ? wmin : w);
+                    double tw;
+                    const int l = bracket_sorted<double>(log(w), s_lw, G19.d3, &tw);
+                    const double v0 = GW.p[0][l] * (1. - tw) + GW.p[0][l + 1] * tw;
+                    const double v1 =
+                        GW.pt.regime >= 2 ? GW.p[1][l] * (1. - tw) + GW.p[1][l + 1] * tw : 0.;
+                    gp19_cell(GW.pt, v0, v1, w, nua + nub, &be, &ba);
                 }
                 else
-                    hr98_kernel(C.hr, nua, nub, &be, &ba);
-            }
-            else if (IMPL == 1)
-                brt06_kernel(C.brt06_pre, T, nua, nub, &be, &ba);
-            else
-                gp19_kernel(G19, nbp, yep, T, nua, nub, &be, &ba);
-            const double Kem[4] = {be, be, be, be};
-            const double Kab[4] = {ba, ba, ba, ba};
-            const double w4 = (nua * nua) * (nub * nub);
-            const double W1 = s_A1[a] * s_A1[b];
-            if (L.stim)
-                add_cell<true>(acc, Kem, Kab, C.g[a], C.g[b], nbb, w4, W1, s_A2[a] * s_A1[b]);
-            else
-                add_cell<false>(acc, Kem, Kab, C.g[a], C.g[b], nbb, w4, W1, s_A2[a] * s_A1[b]);
-            if (a != b)
-            {
+                    gp19_kernel(G19, nbp, yep, T, nua, nub, &be, &ba);
+                const double Kem[4] = {be, be, be, be};
+                const double Kab[4] = {ba, ba, ba, ba};
+                const double w4 = (nua * nua) * (nub * nub);
+                const double W1 = s_A1[a] * s_A1[b];
                 if (L.stim)
-                    add_cell<true>(acc, Kem, Kab, C.g[b], C.g[a], nbb, w4, W1, s_A2[b] * s_A1[a]);
+                    add_cell<true>(acc, Kem, Kab, C.g[a], C.g[b], nbb, w4, W1, s_A2[a] * s_A1[b]);
                 else
-                    add_cell<false>(acc, Kem, Kab, C.g[b], C.g[a], nbb, w4, W1,
-                                    s_A2[b] * s_A1[a]);
+                    add_cell<false>(acc, Kem, Kab, C.g[a], C.g[b], nbb, w4, W1, s_A2[a] * s_A1[b]);
+                if (a != b)
+                {
+                    if (L.stim)
+                        add_cell<true>(acc, Kem, Kab, C.g[b], C.g[a], nbb, w4, W1,
+                                       s_A2[b] * s_A1[a]);
+                    else
+                        add_cell<false>(acc, Kem, Kab, C.g[b], C.g[a], nbb, w4, W1,
+                                        s_A2[b] * s_A1[a]);
+                }
             }
         }
 #pragma unroll
@@ -648,37 +918,45 @@ struct NepsMixed
 {
     dfm::df reta[2][5]; // unreflected F_1..F_5 at eta for e- (0) and e+ (1)
     dfm::df eta[2];
-    float wt[4], invTt[4], etat[4], wf[4], lbf[4], invTf[4], cf[4];
+    float wt[4], wf[4];
+    double invTt[4], etat[4], lbf[4], invTf[4], cf[4]; // exponent arguments in FP64
 };
 
-// TotalNuF (distribution.hpp:298-315) and 1 - TotalNuF in FP32; the blocking
+// TotalNuF (distribution.hpp:298-315) and 1 - TotalNuF in FP32 with the
+// exponent arguments formed in FP64 (they cancel: omega/T_t - eta_t, and
+// log beta_f + c_f log omega - omega/T_f); lw = log omega.  The blocking
 // factor is formed from the complements of the two parts (w_t + w_f = 1 for
 // the reconstructed distribution), so it keeps its relative precision where
 // the occupation approaches 1.
-__device__ __forceinline__ void total_nu_f32(float omega, const NepsMixed& Q, float* g, float* gm)
+__device__ __forceinline__ void total_nu_f32(double omega, double lw, const NepsMixed& Q, float* g,
+                                             float* gm)
 {
-    const float lw = logf(omega);
 #pragma unroll
     for (int s = 0; s < 4; ++s)
     {
-        const float arg = omega * Q.invTt[s] - Q.etat[s];
+        const float arg = (float)fma(omega, Q.invTt[s], -Q.etat[s]);
         const float t   = expf(-fabsf(arg));
         const float inv = 1.f / (t + 1.f);
         const float ft  = arg > 0.f ? t * inv : inv;
         const float ftm = arg > 0.f ? inv : t * inv;
-        const float fn  = expf(Q.lbf[s] + Q.cf[s] * lw - omega * Q.invTf[s]);
+        const float fn  = expf((float)fma(Q.cf[s], lw, fma(-omega, Q.invTf[s], Q.lbf[s])));
         g[s]            = Q.wt[s] * ft + Q.wf[s] * fn;
         gm[s]           = Q.wt[s] * ftm + Q.wf[s] * (1.f - fn);
     }
 }
 
-// NEPSExpFunc (functions.hpp:4401-4413) in FP32; expm1 keeps 1 - e^{-|d|}
+// NEPSExpFunc (functions.hpp:4401-4413) in FP32 for the FP64 argument d;
+// e^{-|d|} takes the FP32 exponential of the rounded argument times the
+// first-order correction for its remainder, expm1 keeps 1 - e^{-|d|}
 // accurate for small |d|.
-__device__ __forceinline__ float neps_exp_f32(float d, bool neg)
+__device__ __forceinline__ float neps_exp_f32(double d, bool neg)
 {
-    const float a  = fabsf(d);
-    const float e  = expf(-a);
-    const float dn = -expm1f(-a) + (d == 0.f ? 1.f : 0.f);
+    const double ad = fabs(d);
+    const float a   = (float)ad;
+    const float alo = (float)(ad - (double)a); // e^{-alo} = 1 - alo to FP32 precision
+    const float ea  = expf(-a);
+    const float e   = ea * (1.f - alo);
+    const float dn  = -expm1f(-a) + ea * alo + (d == 0. ? 1.f : 0.f);
     return (neg ? 1.f : -e) / dn;
 }
 
@@ -697,8 +975,8 @@ __device__ __forceinline__ void neps_item_mixed(const NepsPoint& P, const NepsMi
     const double y = (w < wp) ? w : wp;
     const double d1 = wp - w, d2 = w - wp;
     const bool n1 = signbit(d1) != 0, n2 = signbit(d2) != 0;
-    const float efa = neps_exp_f32((float)d1, n1);
-    const float efb = neps_exp_f32((float)d2, n2);
+    const float efa = neps_exp_f32(d1, n1);
+    const float efb = neps_exp_f32(d2, n2);
     const float sign1 = n1 ? 1.f : -1.f;
     const float sign2 = n2 ? 1.f : -1.f;
 #pragma unroll
@@ -865,6 +1143,12 @@ __global__ void __launch_bounds__(kWarps * 32)
                           (d.temp_f[s] > 0.) && isfinite(d.eta_t[s]) && isfinite(d.beta_f[s]);
             }
             fp32_ok = fp32_ok && isfinite(NP.eta0);
+            // negative pair (+ brem) sums: the outputs cancel, FP64 items
+            if (L.use_pair || L.use_brem)
+            {
+                const double v = lane < 16 ? P->s2d[lane] : 0.;
+                fp32_ok = fp32_ok && __all_sync(0xffffffffu, !(v < 0.));
+            }
         }
         if (!fp32_ok)
             neps_items_fp64(NP, N.d, same_cf, n2, tn, L.stim != 0, nbb, s_x2, s_w2, s_wx, s_wx3,
@@ -882,20 +1166,25 @@ __global__ void __launch_bounds__(kWarps * 32)
                 const int s = lane - 8;
                 const Distr& d = N.d;
                 Q.wt[s]    = (float)d.w_t[s];
-                Q.invTt[s] = (float)(1. / d.temp_t[s]);
-                Q.etat[s]  = (float)d.eta_t[s];
+                Q.invTt[s] = 1. / d.temp_t[s];
+                Q.etat[s]  = d.eta_t[s];
                 Q.wf[s]    = (float)d.w_f[s];
-                Q.lbf[s]   = d.beta_f[s] > 0. ? (float)log(d.beta_f[s]) : -INFINITY;
-                Q.invTf[s] = (float)(1. / d.temp_f[s]);
-                Q.cf[s]    = (float)d.c_f[s];
+                Q.lbf[s]   = d.beta_f[s] > 0. ? log(d.beta_f[s]) : -INFINITY;
+                Q.invTf[s] = 1. / d.temp_f[s];
+                Q.cf[s]    = d.c_f[s];
             }
             __syncwarp();
             const double invT = 1. / T;
+            const double lhtn = log(0.5 * tn);
             dfm::df dacc[16];
 #pragma unroll
             for (int kk = 0; kk < 16; ++kk)
                 dacc[kk] = {0.f, 0.f};
             const int nn2 = n2 * n2;
+            float mag[8];
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk)
+                mag[kk] = 0.f;
             for (int it = lane; it < 2 * nn2; it += 32)
             {
                 const int r   = it >= nn2;
@@ -906,9 +1195,14 @@ __global__ void __launch_bounds__(kWarps * 32)
                 const double w = nu * invT, wp = nub * invT;
                 float em1[4], ab1[4], em2[4], ab2[4];
                 neps_item_mixed(NP, Q, w, wp, em1, ab1, em2, ab2);
+                // log nu, log nubar from the node logarithms (m1_opacities.hpp:880-905)
+                const double lx = L.lx2[i], lm = L.l1m[j], lp = L.l1p[j];
+                const double lnu  = lhtn + (r ? lm - lx : lx + lm);
+                const double lnub = lhtn + (r ? lp - lx : lx + lp);
                 float g[4], gm[4], gb[4], gbm[4];
-                total_nu_f32((float)nu, Q, g, gm);
-                total_nu_f32((float)nub, Q, gb, gbm);
+                total_nu_f32(nu, lnu, Q, g, gm);
+                total_nu_f32(nub, lnub, Q, gb, gbm);
+
                 const float fw = (float)w, fwp = (float)wp;
                 const float w4 = (fw * fwp) * (fw * fwp);
                 const float Wr = (float)((r ? s_wx3[i] : s_wx[i]) * s_w2[j]);
@@ -934,8 +1228,11 @@ __global__ void __launch_bounds__(kWarps * 32)
                         AB2 = w4 * gb[s] * a2;
                         EM2 = w4 * gbm[s] * e2;
                     }
-                    dacc[s]      = dfm::add(dacc[s], Wr * (EM1 + EM2));
-                    dacc[4 + s]  = dfm::add(dacc[4 + s], Wr * (AB1 + AB2));
+                    const float tem = Wr * (EM1 + EM2), tab = Wr * (AB1 + AB2);
+                    dacc[s]      = dfm::add(dacc[s], tem);
+                    dacc[4 + s]  = dfm::add(dacc[4 + s], tab);
+                    mag[s] += fabsf(tem);
+                    mag[4 + s] += fabsf(tab);
                     dacc[8 + s]  = dfm::add(dacc[8 + s], Wr * (fw * EM1 + fwp * EM2));
                     dacc[12 + s] = dfm::add(dacc[12 + s], Wr * (fw * AB1 + fwp * AB2));
                 }
@@ -944,7 +1241,20 @@ __global__ void __launch_bounds__(kWarps * 32)
             const double T4 = (T * T) * (T * T);
 #pragma unroll
             for (int kk = 0; kk < 16; ++kk)
-                acc[kk] = dfm::to_double(dacc[kk]) * NP.pre * T4 * (kk >= 8 ? T : 1.);
+                acc[kk] = dfm::to_double(dacc[kk]);
+            // terms of both signs (occupation above 1): recompute in FP64
+            const bool redo = cancel_factor(acc, mag) > kMaxCancel;
+#pragma unroll
+            for (int kk = 0; kk < 16; ++kk)
+                acc[kk] *= NP.pre * T4 * (kk >= 8 ? T : 1.);
+            if (redo)
+            {
+#pragma unroll
+                for (int kk = 0; kk < 16; ++kk)
+                    acc[kk] = 0.;
+                neps_items_fp64(NP, N.d, same_cf, n2, tn, L.stim != 0, nbb, s_x2, s_w2, s_wx,
+                                s_wx3, lane, acc);
+            }
         }
 #pragma unroll
         for (int kk = 0; kk < 16; ++kk)
