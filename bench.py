@@ -350,12 +350,16 @@ def main():
     top_ms, top_launches = phases[top]
     fp64_peak = bn.fp64_peak_tflops()
     c = consts.get(top, {})
-    pts_per_launch = n * args.steps / max(1, top_launches)
+    # points per launch of the phase (the mixed NES phase is two launches per chunk:
+    # the double-float items and the FP64 items of the points it flags)
+    chunks = -(-n // 16384) * args.steps
+    pts_per_launch = n * args.steps / max(1, chunks)
+    top_launch_ms = top_ms / max(1, chunks)
     roofline = {"kernel": f"grey phase '{top}'", "bound": "fp64", "unit": "TFLOP/s",
                 "achieved": None, "peak": fp64_peak, "frac": None, "traffic": None,
                 "peak_source": "FP64 DFMA-chain probe run in this process "
                                "(bnsn_fp64_peak_probe); not in MEASURED_PEAKS.json",
-                "launch_ms": top_ms / max(1, top_launches), "launches": top_launches,
+                "launch_ms": top_launch_ms, "launches": top_launches,
                 "share_of_step": top_ms / total_ms if total_ms else None}
     if c.get("fp64_flop_per_point"):
         ach = c["fp64_flop_per_point"] * pts_per_launch / (roofline["launch_ms"] * 1e-3) / 1e12

@@ -19,8 +19,9 @@ c_double, c_int, c_bool = ctypes.c_double, ctypes.c_int, ctypes.c_bool
 OK, ERR_ARG, ERR_NQUAD, ERR_CUDA, ERR_NO_TABLE, ERR_NO_DEVICE = range(6)
 FP64, MIXED = 0, 1
 NOALLOC_MAX_POINTS = 4096
-NUM_PHASES = 7
-PHASES = ("prelude", "pair", "brem", "neps", "final", "spectral", "aux")
+NUM_PHASES = 9
+PHASES = ("prelude", "pair", "brem", "neps", "final", "spectral", "aux", "neps_accurate",
+          "neps_fp64")
 BREM_HR98, BREM_BRT06, BREM_GP19 = 0, 1, 2
 
 

@@ -85,6 +85,7 @@ BNSN_DI df add(df a, float b)
 }
 
 BNSN_DI df neg(df a) { return {-a.hi, -a.lo}; }
+BNSN_DI df neg_df(df a) { return {-a.hi, -a.lo}; }
 BNSN_DI df sub(df a, df b) { return add(a, neg(b)); }
 
 BNSN_DI df mul(df a, df b)
@@ -121,6 +122,23 @@ BNSN_DI df div(df a, df b)
     const float q3 = r2.hi * rb;
     const df q     = fast_two_sum(q1, q2);
     return add(q, q3);
+}
+
+// c + t p for the Horner steps of the rational forms: the product error and
+// the addition error are gathered in one correction term (Dekker's addition),
+// 14 FP32 instructions instead of a separate product and accurate sum; the
+// polynomials on [0, 1] have no large internal cancellation.
+BNSN_DI df fma_df(df t, df p, df c)
+{
+    const float ph = t.hi * p.hi;
+    float pe       = fmaf(t.hi, p.hi, -ph);
+    pe             = fmaf(t.hi, p.lo, pe);
+    pe             = fmaf(t.lo, p.hi, pe);
+    const float s  = ph + c.hi;
+    const float bb = s - ph;
+    float e        = (ph - (s - bb)) + (c.hi - bb);
+    e += pe + c.lo;
+    return fast_two_sum(s, e);
 }
 
 // a * 2^k for integer k (exact unless the result leaves the normal range).
@@ -324,7 +342,7 @@ __constant__ FdiTab kFdiTab = {
 #undef BNSN_Z
 
 // r[k-1] = F_k(-|y|), k = 1..5 (the unreflected part of fdi_orders; NaN -> 0).
-BNSN_DI void fdi_raw15(df y, df* r)
+__device__ __noinline__ void fdi_raw15(df y, df* r)
 {
     const df x = (y.hi > 0.f) ? neg(y) : y;
     if (!(x.hi <= 0.f))
@@ -348,17 +366,19 @@ BNSN_DI void fdi_raw15(df y, df* r)
         td = {-0.5f * x.hi, -0.5f * x.lo};
         tn = add(neg(td), 1.f);
     }
+    // terms of the forms: x < -2: 5 (k = 1), 4 (k = 2..5); else 9, 9, 8, 8, 8
 #pragma unroll 1
     for (int k = 0; k < 5; ++k)
     {
         const dfc* cn = kFdiTab.num[reg][k];
         const dfc* cd = kFdiTab.den[reg][k];
-        df pn = mk(cn[8]), pd = mk(cd[8]);
-#pragma unroll
-        for (int i = 7; i >= 0; --i)
+        const int top = reg == 0 ? (k == 0 ? 4 : 3) : (k < 2 ? 8 : 7);
+        df pn = mk(cn[top]), pd = mk(cd[top]);
+#pragma unroll 1
+        for (int i = top - 1; i >= 0; --i)
         {
-            pn = add(mk(cn[i]), mul(tn, pn));
-            pd = add(mk(cd[i]), mul(td, pd));
+            pn = fma_df(tn, pn, mk(cn[i]));
+            pd = fma_df(td, pd, mk(cd[i]));
         }
         const df q = div(pn, pd);
         if (reg == 0)

@@ -59,6 +59,8 @@ enum Phase
     kPhFinal,
     kPhSpectral,
     kPhAux,
+    kPhNepsAccurate, // mixed path: df pass over the points the fast pass flagged
+    kPhNepsFp64,     // mixed path: FP64 pass over the points flagged again
     kNumPhases
 };
 
@@ -68,7 +70,7 @@ void phase_mark(int phase, int end, cudaStream_t stream);
 
 // Grey opacities in chunks of ws_points points; ws holds ws_points per-point
 // scratch records of grey_point_scratch_bytes() (= kGreyRecordBytes) each.
-constexpr size_t kGreyRecordBytes = 766 * sizeof(double);
+constexpr size_t kGreyRecordBytes = 767 * sizeof(double);
 size_t grey_point_scratch_bytes();
 
 // Static scratch of bnsn_m1_opacities_noalloc: room for kNoAllocPoints grey

@@ -61,6 +61,7 @@ struct PointTab
     double snes[16];     // NES/NPS, same layout
     double sbeta[8];     // beta: n_em[2], j_em[2], n_ab[2], j_ab[2]
     double siso[4];      // iso per species
+    double neps_fp64;    // mixed path: 1 if the NES sums of the point must be FP64
 };
 static_assert(sizeof(PointTab) % sizeof(double) == 0, "PointTab must be double words");
 static_assert(sizeof(PointTab) == kGreyRecordBytes, "grey record size");
@@ -427,6 +428,8 @@ __device__ __forceinline__ double cancel_factor(const double* acc, const float* 
 // Mixed sums whose terms cancel by more than this are recomputed in FP64: the
 // FP32 rounding of each term (a few 1e-7) must stay below 1e-6 in the result.
 constexpr double kMaxCancel = 2.0;
+// The accurate (all-df) pass keeps ~1e-13 per term.
+constexpr double kMaxCancelDf = 1e5;
 
 // add_cell in FP32 for a species-independent kernel (brem): K_em, K_ab are
 // dimensionless, w4 = (y_a y_b)^2; the caller scales by T^4 and the kernel's
@@ -1082,14 +1085,171 @@ __device__ __forceinline__ void neps_item_mixed(const NepsPoint& P, const NepsMi
     }
 }
 
-template <bool MIXED>
+// MIXED: double-float items, FP64 points flagged for the second launch.
+// !MIXED: FP64 items (all points, or with FP64_ONLY_FLAGGED only the points the
+// mixed launch flagged).
+// TotalNuF and 1 - TotalNuF in df (the accurate pass of the mixed path).
+__device__ __forceinline__ void total_nu_df(double omega, double lw, const NepsMixed& Q,
+                                            const double* wt, const double* wf, dfm::df* g,
+                                            dfm::df* gm)
+{
+    using namespace dfm;
+#pragma unroll 1
+    for (int s = 0; s < 4; ++s)
+    {
+        const double arg = fma(omega, Q.invTt[s], -Q.etat[s]);
+        const df t       = exp_df(from_double(-fabs(arg)));
+        const df inv     = div(mk(1.f), add(t, 1.f));
+        const df ti      = mul(t, inv);
+        const df ft = arg > 0. ? ti : inv, ftm = arg > 0. ? inv : ti;
+        const df fn = exp_df(from_double(fma(Q.cf[s], lw, fma(-omega, Q.invTf[s], Q.lbf[s]))));
+        const df Wt = from_double(wt[s]), Wf = from_double(wf[s]);
+        g[s]  = add(mul(Wt, ft), mul(Wf, fn));
+        gm[s] = add(mul(Wt, ftm), mul(Wf, add(neg(fn), 1.f)));
+    }
+}
+
+// NEPSExpFunc in df.
+__device__ __forceinline__ dfm::df neps_exp_df(double d, bool negd)
+{
+    using namespace dfm;
+    const df e  = exp_df(from_double(-fabs(d)));
+    const df dn = add(add(neg(e), 1.f), d == 0. ? 1.f : 0.f);
+    return div(negd ? mk(1.f) : neg(e), dn);
+}
+
+// neps_item_mixed with every product after the Fermi integrals in df.
+__device__ __forceinline__ void neps_item_df(const NepsPoint& P, const NepsMixed& Q, double w,
+                                             double wp, dfm::df* em1, dfm::df* ab1, dfm::df* em2,
+                                             dfm::df* ab2)
+{
+    using namespace dfm;
+    const double x = (w > wp) ? w : wp;
+    const double y = (w < wp) ? w : wp;
+    const double d1 = wp - w, d2 = w - wp;
+    const bool n1 = signbit(d1) != 0, n2 = signbit(d2) != 0;
+    const df efa = neps_exp_df(d1, n1);
+    const df efb = neps_exp_df(d2, n2);
+    const float sign1 = n1 ? 1.f : -1.f;
+    const float sign2 = n2 ? 1.f : -1.f;
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+        em1[s] = ab1[s] = em2[s] = ab2[s] = {0.f, 0.f};
+    const df W  = from_double(w), WP = from_double(wp);
+    const df S  = add(W, WP);
+    const df Pp = mul(W, WP);
+    const df Dn = mul(Pp, Pp);
+    const df X  = from_double(x), Y = from_double(y);
+#pragma unroll 1
+    for (int e = 0; e < 2; ++e)
+    {
+        const double eta = e ? P.eta1 : P.eta0;
+        df r1[4], r2[4];
+        if (y > eta * 1e-3)
+        {
+            const df aw = from_double(eta - w), awp = from_double(eta - wp);
+            const double adw = fabs(w - wp);
+            const df aab = from_double(eta - adw);
+            df rw[5], rwp[5], rab[5];
+            fdi_raw15(aw, rw);
+            fdi_raw15(awp, rwp);
+            fdi_raw15(aab, rab);
+            df dw[5], d5[5];
+            fdi_diff15(rw, rwp, aw, awp, from_double(w - wp), dw);
+            fdi_diff15(rab, Q.reta[e], aab, Q.eta[e], from_double(adw), d5);
+            const df dabs[3] = {d5[2], d5[3], d5[4]};
+            const df T1 = add(dw[3], mul(add(mul(S, dw[2]), mul(mul(Pp, 3.f), dw[1])), 2.f));
+            const df U  = add(mul(X, dabs[1]), mul(mul(mul(X, X), 2.f), dabs[0]));
+            const df V  = add(neg(mul(Y, dabs[1])), mul(mul(mul(Y, Y), 2.f), dabs[0]));
+            const df ST = mul(S, T1);
+            constexpr dfc kFifth(0.2);
+            const df dd2 = mul(dabs[2], mk(kFifth)), dw4 = mul(dw[4], mk(kFifth));
+            const df c1 = sub(mul(dd2, sign1), dw4);
+            const df c2 = add(mul(dd2, sign2), dw4);
+            const df s6 = mul(dw[0], 6.f);
+            const df A1 = sub(div(add(sub(c1, ST), mul(U, sign1)), Dn), s6);
+            const df B1 = div(add(c1, mul(V, sign1)), Dn);
+            const df A2 = add(div(add(add(c2, ST), mul(U, sign2)), Dn), s6);
+            const df B2 = div(add(c2, mul(V, sign2)), Dn);
+            constexpr dfc kBp(k::NepsBPlus), kBm(k::NepsBMinus), kBz(k::NepsBZero);
+#pragma unroll
+            for (int s = 0; s < 4; ++s)
+            {
+                const df bo      = (s < 2) ? mk(kBp) : mk(kBm);
+                const bool first = ((s & 1) == 0) != (e == 1);
+                r1[s] = first ? add(mul(A1, bo), mul(B1, mk(kBz))) : add(mul(A1, mk(kBz)), mul(B1, bo));
+                r2[s] = first ? add(mul(A2, bo), mul(B2, mk(kBz))) : add(mul(A2, mk(kBz)), mul(B2, bo));
+            }
+        }
+        else
+        {
+            const double* f0e = e ? P.fe1 : P.fe0;
+            const double fd0  = e ? P.fd01 : P.fd00;
+            if (x > eta * 1e-3)
+            {
+                double fx[3];
+                fdi_orders<0, 2>(eta - x, fx);
+                const double f[5] = {fx[2] - f0e[2], fx[1], f0e[1],
+                                     fx[0] + y * fermi_distr(0., 1., eta - x) / 6.,
+                                     f0e[0] - y * fd0 / 6.};
+#pragma unroll
+                for (int s = 0; s < 4; ++s)
+                {
+                    double b1, b2;
+                    neps_couplings(e, s, &b1, &b2);
+                    r1[s] = from_double(mb_int_one(x, y, (int)sign1, b1, b2, f));
+                    r2[s] = from_double(mb_int_one(x, y, (int)sign2, b1, b2, f));
+                }
+            }
+            else
+            {
+                const double f[3] = {fd0, f0e[0], f0e[1]};
+#pragma unroll
+                for (int s = 0; s < 4; ++s)
+                {
+                    double b1, b2;
+                    neps_couplings(e, s, &b1, &b2);
+                    r1[s] = from_double(mb_int_two(w, wp, x, y, b1, b2, f));
+                    r2[s] = from_double(mb_int_two(wp, w, x, y, b1, b2, f));
+                }
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < 4; ++s)
+        {
+            em1[s] = sub(em1[s], mul(r1[s], efb));
+            ab1[s] = add(ab1[s], mul(r1[s], efa));
+            em2[s] = sub(em2[s], mul(r2[s], efa));
+            ab2[s] = add(ab2[s], mul(r2[s], efb));
+        }
+    }
+}
+
+// NES launch modes.  The plain path runs kNesFp64All.  The mixed path runs
+// three launches per chunk, each over all points but working only on its own:
+//   kNesFast      double-float Fermi integrals, FP32 weights; flags a point 1
+//                 when its sums cancel (terms of both signs, or negative pair +
+//                 brem sums) and 2 when it leaves the FP32/df range envelope;
+//   kNesAccurate  flag 1: every product in df (cancellation up to ~1e5);
+//                 beyond that the point is flagged 2;
+//   kNesFp64Flag  flag 2: FP64 items.
+enum NesMode
+{
+    kNesFp64All = 0,
+    kNesFast,
+    kNesAccurate,
+    kNesFp64Flag
+};
+
+template <int MODE>
 __global__ void __launch_bounds__(kWarps * 32)
     grey_neps_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
                      double* __restrict__ scratch)
 {
+    constexpr bool MIX = MODE == kNesFast || MODE == kNesAccurate;
     __shared__ double s_x2[kMaxQ], s_w2[kMaxQ], s_wx[kMaxQ], s_wx3[kMaxQ];
     __shared__ NepsTab s_nt[kWarps];
-    __shared__ NepsMixed s_nm[MIXED ? kWarps : 1];
+    __shared__ NepsMixed s_nm[MIX ? kWarps : 1];
     for (int k = threadIdx.x; k < kMaxQ; k += blockDim.x)
     {
         s_x2[k]  = L.x2[k];
@@ -1099,16 +1259,21 @@ __global__ void __launch_bounds__(kWarps * 32)
     }
     __syncthreads();
     const int lane = threadIdx.x & 31;
-    NepsTab& N     = s_nt[threadIdx.x >> 5];
+    const int wid  = threadIdx.x >> 5;
+    NepsTab& N     = s_nt[wid];
     const int n2   = L.n2;
     const bool nbb = L.neglect_blocking != 0;
     const int64_t nwarp = (int64_t)gridDim.x * kWarps;
 
-    for (int64_t q = (int64_t)blockIdx.x * kWarps + (threadIdx.x >> 5); q < np; q += nwarp)
+    for (int64_t q = (int64_t)blockIdx.x * kWarps + wid; q < np; q += nwarp)
     {
         const int64_t p = p0 + q;
         PointTab* P     = (PointTab*)(scratch + q * kTabWords);
-        const double T  = L.eos[1][p], mu_e = L.eos[7][p];
+        if (MODE == kNesAccurate && P->neps_fp64 != 1.)
+            continue;
+        if (MODE == kNesFp64Flag && P->neps_fp64 != 2.)
+            continue;
+        const double T = L.eos[1][p], mu_e = L.eos[7][p];
         __syncwarp();
         warp_copy((double*)&N.d, (const double*)&P->d, 28 + 12 + 2, lane);
         if (lane == 0)
@@ -1129,132 +1294,192 @@ __global__ void __launch_bounds__(kWarps * 32)
 #pragma unroll
         for (int kk = 0; kk < 16; ++kk)
             acc[kk] = 0.;
-        // FP32 range envelope of the mixed item loop: the occupation of every
-        // species must stay far above the FP32 normal range at its peak.
-        bool fp32_ok = MIXED;
-        if (MIXED)
+        if (!MIX)
         {
-#pragma unroll
-            for (int s = 0; s < 4; ++s)
-            {
-                const Distr& d = N.d;
-                fp32_ok = fp32_ok && (d.w_t[s] == 0. || d.eta_t[s] > -60.) &&
-                          (d.w_f[s] == 0. || d.beta_f[s] > 1e-30) && (d.temp_t[s] > 0.) &&
-                          (d.temp_f[s] > 0.) && isfinite(d.eta_t[s]) && isfinite(d.beta_f[s]);
-            }
-            fp32_ok = fp32_ok && isfinite(NP.eta0);
-            // negative pair (+ brem) sums: the outputs cancel, FP64 items
-            if (L.use_pair || L.use_brem)
-            {
-                const double v = lane < 16 ? P->s2d[lane] : 0.;
-                fp32_ok = fp32_ok && __all_sync(0xffffffffu, !(v < 0.));
-            }
-        }
-        if (!fp32_ok)
             neps_items_fp64(NP, N.d, same_cf, n2, tn, L.stim != 0, nbb, s_x2, s_w2, s_wx, s_wx3,
                             lane, acc);
+        }
         else
         {
-            NepsMixed& Q = s_nm[MIXED ? (threadIdx.x >> 5) : 0];
-            if (lane < 2)
+            int flag = 0;
+            if (MODE == kNesFast)
             {
-                Q.eta[lane] = dfm::from_double(lane ? NP.eta1 : NP.eta0);
-                dfm::fdi_raw15(Q.eta[lane], Q.reta[lane]);
-            }
-            else if (lane >= 8 && lane < 12)
-            {
-                const int s = lane - 8;
-                const Distr& d = N.d;
-                Q.wt[s]    = (float)d.w_t[s];
-                Q.invTt[s] = 1. / d.temp_t[s];
-                Q.etat[s]  = d.eta_t[s];
-                Q.wf[s]    = (float)d.w_f[s];
-                Q.lbf[s]   = d.beta_f[s] > 0. ? log(d.beta_f[s]) : -INFINITY;
-                Q.invTf[s] = 1. / d.temp_f[s];
-                Q.cf[s]    = d.c_f[s];
-            }
-            __syncwarp();
-            const double invT = 1. / T;
-            const double lhtn = log(0.5 * tn);
-            dfm::df dacc[16];
-#pragma unroll
-            for (int kk = 0; kk < 16; ++kk)
-                dacc[kk] = {0.f, 0.f};
-            const int nn2 = n2 * n2;
-            float mag[8];
-#pragma unroll
-            for (int kk = 0; kk < 8; ++kk)
-                mag[kk] = 0.f;
-            for (int it = lane; it < 2 * nn2; it += 32)
-            {
-                const int r   = it >= nn2;
-                const int rem = it - r * nn2;
-                const int i = rem / n2, j = rem - (rem / n2) * n2;
-                double nu, nub;
-                neps_energies(r, s_x2[i], s_x2[j], tn, &nu, &nub);
-                const double w = nu * invT, wp = nub * invT;
-                float em1[4], ab1[4], em2[4], ab2[4];
-                neps_item_mixed(NP, Q, w, wp, em1, ab1, em2, ab2);
-                // log nu, log nubar from the node logarithms (m1_opacities.hpp:880-905)
-                const double lx = L.lx2[i], lm = L.l1m[j], lp = L.l1p[j];
-                const double lnu  = lhtn + (r ? lm - lx : lx + lm);
-                const double lnub = lhtn + (r ? lp - lx : lx + lp);
-                float g[4], gm[4], gb[4], gbm[4];
-                total_nu_f32(nu, lnu, Q, g, gm);
-                total_nu_f32(nub, lnub, Q, gb, gbm);
-
-                const float fw = (float)w, fwp = (float)wp;
-                const float w4 = (fw * fwp) * (fw * fwp);
-                const float Wr = (float)((r ? s_wx3[i] : s_wx[i]) * s_w2[j]);
+                // range envelope: the occupation of every species must stay far
+                // above the FP32 normal range at its peak
+                bool ok = isfinite(NP.eta0);
 #pragma unroll
                 for (int s = 0; s < 4; ++s)
                 {
-                    const float e1 = em1[s] * gb[s];
-                    const float a1 = ab1[s] * (nbb ? 1.f : gbm[s]);
-                    const float e2 = em2[s] * g[s];
-                    const float a2 = ab2[s] * (nbb ? 1.f : gm[s]);
-                    float EM1, AB1, EM2, AB2;
-                    if (L.stim)
+                    const Distr& d = N.d;
+                    ok = ok && (d.w_t[s] == 0. || d.eta_t[s] > -60.) &&
+                         (d.w_f[s] == 0. || d.beta_f[s] > 1e-30) && (d.temp_t[s] > 0.) &&
+                         (d.temp_f[s] > 0.) && isfinite(d.eta_t[s]) && isfinite(d.beta_f[s]);
+                }
+                if (!ok)
+                    flag = 2;
+                else if (L.use_pair || L.use_brem)
+                {
+                    // negative pair (+ brem) sums: the outputs cancel
+                    const double v = lane < 16 ? P->s2d[lane] : 0.;
+                    if (!__all_sync(0xffffffffu, !(v < 0.)))
+                        flag = 1;
+                }
+            }
+            if (flag == 0)
+            {
+                NepsMixed& Q = s_nm[MIX ? wid : 0];
+                if (lane < 2)
+                {
+                    Q.eta[lane] = dfm::from_double(lane ? NP.eta1 : NP.eta0);
+                    dfm::fdi_raw15(Q.eta[lane], Q.reta[lane]);
+                }
+                else if (lane >= 8 && lane < 12)
+                {
+                    const int s    = lane - 8;
+                    const Distr& d = N.d;
+                    Q.wt[s]    = (float)d.w_t[s];
+                    Q.invTt[s] = 1. / d.temp_t[s];
+                    Q.etat[s]  = d.eta_t[s];
+                    Q.wf[s]    = (float)d.w_f[s];
+                    Q.lbf[s]   = d.beta_f[s] > 0. ? log(d.beta_f[s]) : -INFINITY;
+                    Q.invTf[s] = 1. / d.temp_f[s];
+                    Q.cf[s]    = d.c_f[s];
+                }
+                __syncwarp();
+                const double invT = 1. / T;
+                const double lhtn = log(0.5 * tn);
+                dfm::df dacc[16];
+#pragma unroll
+                for (int kk = 0; kk < 16; ++kk)
+                    dacc[kk] = {0.f, 0.f};
+                float mag[8];
+#pragma unroll
+                for (int kk = 0; kk < 8; ++kk)
+                    mag[kk] = 0.f;
+                const int nn2 = n2 * n2;
+                for (int it = lane; it < 2 * nn2; it += 32)
+                {
+                    const int r   = it >= nn2;
+                    const int rem = it - r * nn2;
+                    const int i = rem / n2, j = rem - (rem / n2) * n2;
+                    double nu, nub;
+                    neps_energies(r, s_x2[i], s_x2[j], tn, &nu, &nub);
+                    const double w = nu * invT, wp = nub * invT;
+                    // log nu, log nubar from the node logarithms
+                    const double lx = L.lx2[i], lm = L.l1m[j], lp = L.l1p[j];
+                    const double lnu  = lhtn + (r ? lm - lx : lx + lm);
+                    const double lnub = lhtn + (r ? lp - lx : lx + lp);
+                    const double Wr   = (r ? s_wx3[i] : s_wx[i]) * s_w2[j];
+                    if (MODE == kNesFast)
                     {
-                        AB1 = w4 * g[s] * (e1 + a1);
-                        EM1 = w4 * e1;
-                        AB2 = w4 * gb[s] * (e2 + a2);
-                        EM2 = w4 * e2;
+                        float em1[4], ab1[4], em2[4], ab2[4];
+                        neps_item_mixed(NP, Q, w, wp, em1, ab1, em2, ab2);
+                        float g[4], gm[4], gb[4], gbm[4];
+                        total_nu_f32(nu, lnu, Q, g, gm);
+                        total_nu_f32(nub, lnub, Q, gb, gbm);
+                        const float fw = (float)w, fwp = (float)wp;
+                        const float w4 = (fw * fwp) * (fw * fwp);
+                        const float Wf = (float)Wr;
+#pragma unroll
+                        for (int s = 0; s < 4; ++s)
+                        {
+                            const float e1 = em1[s] * gb[s];
+                            const float a1 = ab1[s] * (nbb ? 1.f : gbm[s]);
+                            const float e2 = em2[s] * g[s];
+                            const float a2 = ab2[s] * (nbb ? 1.f : gm[s]);
+                            float EM1, AB1, EM2, AB2;
+                            if (L.stim)
+                            {
+                                AB1 = w4 * g[s] * (e1 + a1);
+                                EM1 = w4 * e1;
+                                AB2 = w4 * gb[s] * (e2 + a2);
+                                EM2 = w4 * e2;
+                            }
+                            else
+                            {
+                                AB1 = w4 * g[s] * a1;
+                                EM1 = w4 * gm[s] * e1;
+                                AB2 = w4 * gb[s] * a2;
+                                EM2 = w4 * gbm[s] * e2;
+                            }
+                            const float tem = Wf * (EM1 + EM2), tab = Wf * (AB1 + AB2);
+                            dacc[s]      = dfm::add(dacc[s], tem);
+                            dacc[4 + s]  = dfm::add(dacc[4 + s], tab);
+                            dacc[8 + s]  = dfm::add(dacc[8 + s], Wf * (fw * EM1 + fwp * EM2));
+                            dacc[12 + s] = dfm::add(dacc[12 + s], Wf * (fw * AB1 + fwp * AB2));
+                            mag[s] += fabsf(tem);
+                            mag[4 + s] += fabsf(tab);
+                        }
                     }
                     else
                     {
-                        AB1 = w4 * g[s] * a1;
-                        EM1 = w4 * gm[s] * e1;
-                        AB2 = w4 * gb[s] * a2;
-                        EM2 = w4 * gbm[s] * e2;
+                        using namespace dfm;
+                        df em1[4], ab1[4], em2[4], ab2[4];
+                        neps_item_df(NP, Q, w, wp, em1, ab1, em2, ab2);
+                        double wt[4], wfd[4];
+#pragma unroll
+                        for (int s = 0; s < 4; ++s)
+                        {
+                            wt[s]  = N.d.w_t[s];
+                            wfd[s] = N.d.w_f[s];
+                        }
+                        df g[4], gm[4], gb[4], gbm[4];
+                        total_nu_df(nu, lnu, Q, wt, wfd, g, gm);
+                        total_nu_df(nub, lnub, Q, wt, wfd, gb, gbm);
+                        const df W = from_double(w), WP = from_double(wp);
+                        const df ww = mul(W, WP), w4 = mul(ww, ww), Wd = from_double(Wr);
+#pragma unroll
+                        for (int s = 0; s < 4; ++s)
+                        {
+                            const df e1 = mul(em1[s], gb[s]);
+                            const df a1 = nbb ? ab1[s] : mul(ab1[s], gbm[s]);
+                            const df e2 = mul(em2[s], g[s]);
+                            const df a2 = nbb ? ab2[s] : mul(ab2[s], gm[s]);
+                            df EM1, AB1, EM2, AB2;
+                            if (L.stim)
+                            {
+                                AB1 = mul(mul(w4, g[s]), add(e1, a1));
+                                EM1 = mul(w4, e1);
+                                AB2 = mul(mul(w4, gb[s]), add(e2, a2));
+                                EM2 = mul(w4, e2);
+                            }
+                            else
+                            {
+                                AB1 = mul(mul(w4, g[s]), a1);
+                                EM1 = mul(mul(w4, gm[s]), e1);
+                                AB2 = mul(mul(w4, gb[s]), a2);
+                                EM2 = mul(mul(w4, gbm[s]), e2);
+                            }
+                            const df tem = mul(Wd, add(EM1, EM2)), tab = mul(Wd, add(AB1, AB2));
+                            dacc[s]      = add(dacc[s], tem);
+                            dacc[4 + s]  = add(dacc[4 + s], tab);
+                            dacc[8 + s]  = add(dacc[8 + s], mul(Wd, add(mul(W, EM1), mul(WP, EM2))));
+                            dacc[12 + s] = add(dacc[12 + s], mul(Wd, add(mul(W, AB1), mul(WP, AB2))));
+                            mag[s] += fabsf(tem.hi);
+                            mag[4 + s] += fabsf(tab.hi);
+                        }
                     }
-                    const float tem = Wr * (EM1 + EM2), tab = Wr * (AB1 + AB2);
-                    dacc[s]      = dfm::add(dacc[s], tem);
-                    dacc[4 + s]  = dfm::add(dacc[4 + s], tab);
-                    mag[s] += fabsf(tem);
-                    mag[4 + s] += fabsf(tab);
-                    dacc[8 + s]  = dfm::add(dacc[8 + s], Wr * (fw * EM1 + fwp * EM2));
-                    dacc[12 + s] = dfm::add(dacc[12 + s], Wr * (fw * AB1 + fwp * AB2));
                 }
-            }
-            // back to the FP64 layout: sums x pre T^4 (x T for the energy moments)
-            const double T4 = (T * T) * (T * T);
-#pragma unroll
-            for (int kk = 0; kk < 16; ++kk)
-                acc[kk] = dfm::to_double(dacc[kk]);
-            // terms of both signs (occupation above 1): recompute in FP64
-            const bool redo = cancel_factor(acc, mag) > kMaxCancel;
-#pragma unroll
-            for (int kk = 0; kk < 16; ++kk)
-                acc[kk] *= NP.pre * T4 * (kk >= 8 ? T : 1.);
-            if (redo)
-            {
 #pragma unroll
                 for (int kk = 0; kk < 16; ++kk)
-                    acc[kk] = 0.;
-                neps_items_fp64(NP, N.d, same_cf, n2, tn, L.stim != 0, nbb, s_x2, s_w2, s_wx,
-                                s_wx3, lane, acc);
+                    acc[kk] = dfm::to_double(dacc[kk]);
+                // terms of both signs (occupation above 1): the fast pass hands
+                // the point to the accurate pass, the accurate pass to FP64
+                const double amp = cancel_factor(acc, mag);
+                if (amp > (MODE == kNesFast ? kMaxCancel : kMaxCancelDf))
+                    flag = MODE == kNesFast ? 1 : 2;
+                const double T4 = (T * T) * (T * T);
+#pragma unroll
+                for (int kk = 0; kk < 16; ++kk)
+                    acc[kk] *= NP.pre * T4 * (kk >= 8 ? T : 1.);
             }
+            if (MODE == kNesFast || flag != 0)
+            {
+                if (lane == 0)
+                    P->neps_fp64 = (double)flag;
+            }
+            if (flag != 0)
+                continue; // a later launch writes this point's sums
         }
 #pragma unroll
         for (int kk = 0; kk < 16; ++kk)
@@ -1416,14 +1641,32 @@ cudaError_t launch_grey(const OpacityLaunch& L, cudaStream_t st, int sms, double
         }
         if (L.use_inel)
         {
-            phase_mark(kPhNeps, 0, st);
             if (L.mixed)
-                grey_neps_kernel<true><<<grid_for(grey_neps_kernel<true>, kWarps * 32, wb, sms),
-                                         kWarps * 32, 0, st>>>(L, p0, np, ws);
+            {
+                phase_mark(kPhNeps, 0, st);
+                grey_neps_kernel<kNesFast>
+                    <<<grid_for(grey_neps_kernel<kNesFast>, kWarps * 32, wb, sms), kWarps * 32, 0,
+                       st>>>(L, p0, np, ws);
+                phase_mark(kPhNeps, 1, st);
+                phase_mark(kPhNepsAccurate, 0, st);
+                grey_neps_kernel<kNesAccurate>
+                    <<<grid_for(grey_neps_kernel<kNesAccurate>, kWarps * 32, wb, sms), kWarps * 32,
+                       0, st>>>(L, p0, np, ws);
+                phase_mark(kPhNepsAccurate, 1, st);
+                phase_mark(kPhNepsFp64, 0, st);
+                grey_neps_kernel<kNesFp64Flag>
+                    <<<grid_for(grey_neps_kernel<kNesFp64Flag>, kWarps * 32, wb, sms), kWarps * 32,
+                       0, st>>>(L, p0, np, ws);
+                phase_mark(kPhNepsFp64, 1, st);
+            }
             else
-                grey_neps_kernel<false><<<grid_for(grey_neps_kernel<false>, kWarps * 32, wb, sms),
-                                          kWarps * 32, 0, st>>>(L, p0, np, ws);
-            phase_mark(kPhNeps, 1, st);
+            {
+                phase_mark(kPhNeps, 0, st);
+                grey_neps_kernel<kNesFp64All>
+                    <<<grid_for(grey_neps_kernel<kNesFp64All>, kWarps * 32, wb, sms), kWarps * 32,
+                       0, st>>>(L, p0, np, ws);
+                phase_mark(kPhNeps, 1, st);
+            }
         }
         phase_mark(kPhFinal, 0, st);
         grey_final_kernel<<<grid_for(grey_final_kernel, 128, (np + 127) / 128, sms), 128, 0, st>>>(

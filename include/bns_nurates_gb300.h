@@ -404,10 +404,12 @@ int bnsn_fp64_peak_probe(int64_t iters, double* tflops);
  * recorded events, adds each launch's duration to ms[phase] and its count to
  * launches[phase] (arrays of BNSN_NUM_PHASES entries, accumulated since the
  * previous bnsn_phase_times call), and clears the record.  Phases:
- * 0 grey prelude, 1 pair cells, 2 brem cells, 3 NES/NPS pairs, 4 grey
- * assembly, 5 spectral, 6 distribution/equilibrium.  Timing one device at a
- * time is supported. */
-#define BNSN_NUM_PHASES 7
+ * 0 grey prelude, 1 pair cells, 2 brem cells, 3 NES/NPS pairs (mixed path:
+ * the fast pass), 4 grey assembly, 5 spectral, 6 distribution/equilibrium,
+ * 7 mixed NES double-float pass over flagged points, 8 mixed NES FP64 pass
+ * over the points flagged again.  Timing one device at a time is
+ * supported. */
+#define BNSN_NUM_PHASES 9
 int bnsn_phase_timing(int enable);
 int bnsn_phase_times(double* ms, int64_t* launches);
 /* Number of kernels this library has launched in the process. */
