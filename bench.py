@@ -342,35 +342,37 @@ def main():
                "call": "bnsn_m1_opacities_host"}
         assert np.array_equal(o_np, res), "host-buffer and device paths differ"
 
-    # roofline of the dominant kernel phase
+    # roofline of the dominant kernel phase: its pipe (FP64 for the plain path,
+    # FP32 for the mixed path's double-float phases) and its work per point from
+    # an ncu instruction count (profiles/bench_constants.json)
     peaks = load_json("MEASURED_PEAKS.json")
     consts = load_json("profiles", "bench_constants.json").get(args.workload, {}).get(
         args.precision, {})
     top = max(phases, key=lambda k: phases[k][0])
     top_ms, top_launches = phases[top]
-    fp64_peak = bn.fp64_peak_tflops()
     c = consts.get(top, {})
-    # points per launch of the phase (the mixed NES phase is two launches per chunk:
-    # the double-float items and the FP64 items of the points it flags)
-    chunks = -(-n // 16384) * args.steps
+    bound = c.get("bound", "fp64")
+    probe = bn.fp64_peak_tflops if bound == "fp64" else bn.fp32_peak_tflops
+    peak = probe()
+    chunks = -(-n // 16384) * args.steps       # launches of the phase: one per scratch chunk
     pts_per_launch = n * args.steps / max(1, chunks)
     top_launch_ms = top_ms / max(1, chunks)
-    roofline = {"kernel": f"grey phase '{top}'", "bound": "fp64", "unit": "TFLOP/s",
-                "achieved": None, "peak": fp64_peak, "frac": None, "traffic": None,
-                "peak_source": "FP64 DFMA-chain probe run in this process "
-                               "(bnsn_fp64_peak_probe); not in MEASURED_PEAKS.json",
+    roofline = {"kernel": f"grey phase '{top}'", "bound": bound, "unit": "TFLOP/s",
+                "achieved": None, "peak": peak, "frac": None, "traffic": None,
+                "peak_source": f"{bound.upper()} FMA-chain probe run in this process "
+                               f"(bnsn_{bound}_peak_probe); MEASURED_PEAKS.json has no "
+                               f"{bound.upper()} figure",
                 "launch_ms": top_launch_ms, "launches": top_launches,
                 "share_of_step": top_ms / total_ms if total_ms else None}
-    if c.get("fp64_flop_per_point"):
-        ach = c["fp64_flop_per_point"] * pts_per_launch / (roofline["launch_ms"] * 1e-3) / 1e12
+    work = c.get(f"{bound}_flop_per_point")
+    if work:
+        ach = work * pts_per_launch / (top_launch_ms * 1e-3) / 1e12
         roofline["achieved"] = ach
-        roofline["frac"] = ach / fp64_peak if fp64_peak else None
+        roofline["frac"] = ach / peak if peak else None
+        roofline["work_per_point"] = work
         roofline["work_source"] = c.get("source")
     if c.get("dram_bytes_per_point"):
         roofline["traffic"] = c["dram_bytes_per_point"] * pts_per_launch
-    if c.get("fp32_flop_per_point"):
-        roofline["fp32_tflops"] = (c["fp32_flop_per_point"] * pts_per_launch /
-                                   (roofline["launch_ms"] * 1e-3) / 1e12)
     hbm = peaks.get("hbm_gbs")
     io_gbs = (23 + 20) * 8 * n / (ms_per_step * 1e-3) / 1e9
     roofline["hbm_secondary"] = {"achieved_gbs": io_gbs, "peak_gbs": hbm,

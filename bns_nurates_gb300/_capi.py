@@ -143,6 +143,7 @@ SIGNATURES = {
     "bnsn_synthetic_points": (c_int, [ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64, P, P,
                                       c_int]),
     "bnsn_fp64_peak_probe": (c_int, [ctypes.c_int64, P]),
+    "bnsn_fp32_peak_probe": (c_int, [ctypes.c_int64, P]),
     "bnsn_phase_timing": (c_int, [c_int]),
     "bnsn_phase_times": (c_int, [P, P]),
     "bnsn_kernel_launches": (ctypes.c_int64, []),

@@ -230,6 +230,13 @@ def fp64_peak_tflops(iters=1 << 16):
     return v.value
 
 
+def fp32_peak_tflops(iters=1 << 18):
+    """Measured FP32 FMA throughput of the current device (TFLOP/s)."""
+    v = ctypes.c_double()
+    _check(C.load().bnsn_fp32_peak_probe(int(iters), ctypes.byref(v)))
+    return v.value
+
+
 def phase_timing(enable):
     """Bracket every library kernel launch with CUDA events (diagnostic)."""
     _check(C.load().bnsn_phase_timing(int(bool(enable))))

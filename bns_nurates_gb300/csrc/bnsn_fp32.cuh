@@ -51,6 +51,23 @@ BNSN_DI void hr98_mixed_from(const fp64::Hr98Point& P, Hr98Mixed* M)
     M->outer = 3. * k::BremConst / P.mcorr;
 }
 
+// x^p for x > 0 to about 1 ulp: log2 x = k + log2 m with the binary exponent
+// k exact and m in [1, 2); p log2 x is carried as hi + lo (exact product of p
+// and k), split into an integer n and a fraction f, and x^p = 2^n exp2(f).
+// exp(p log x) in FP32 loses |p log x| ulps in the rounded argument.
+BNSN_DI float powf_acc(float x, float p)
+{
+    int k;
+    const float m  = frexpf(x, &k); // x = m 2^k, m in [0.5, 1)
+    const float lm = log2f(m);      // in [-1, 0)
+    const float kf = (float)k;
+    const float hi = p * kf;
+    const float lo = fmaf(p, kf, -hi) + p * lm; // p k - hi exactly, plus p log2 m
+    const float n  = rintf(hi);
+    const float f  = (hi - n) + lo;             // hi - n exact
+    return ldexpf(exp2f(f), (int)n);
+}
+
 // Sum over the three NN channels of n gamma S(x) / (T (x^2 + (gamma g/2)^2)).
 // The interpolation (s_nd^-p + s_d^-p)^(-1/p) of Eq.(49) is evaluated as
 // min * (1 + (max/min)^-p)^(-1/p): the same value, but the outer power acts on
@@ -66,11 +83,10 @@ BNSN_DI float hr98_shape(const Hr98Mixed& M, float x_in)
                       ((float)k::SqrtPi + (q * q) * (q * q));
     const float em1 = -expm1f(-x);
     const float X2  = x * x + (float)k::FourPiSq;
-    const float lx  = logf(x);
-    const float px11  = expf(1.1f * lx);
-    const float px093 = expf(0.93f * lx);
-    const float px12  = expf(1.2f * lx);
-    const float px28  = expf(2.8f * lx);
+    const float px11  = powf_acc(x, 1.1f);
+    const float px093 = powf_acc(x, 0.93f);
+    const float px12  = powf_acc(x, 1.2f);
+    const float px28  = powf_acc(x, 2.8f);
     const float x2    = x * x;
     const float xterm = 3.f + (x - 1.2f) * (x - 1.2f) + 1.f / (x2 * x2);
     const float gpart = 0.0044f * px11 * y / M.Dy;
@@ -83,7 +99,7 @@ BNSN_DI float hr98_shape(const Hr98Mixed& M, float x_in)
         const float s_d    = M.K1[c] * X2 * x * M.f_u[c] / ((float)k::FourPiSq * em1);
         const float lo     = fminf(snd, s_d);
         const float hi     = fmaxf(snd, s_d);
-        const float t      = expf(-M.p * logf(hi / lo));
+        const float t      = powf_acc(hi / lo, -M.p);
         const float s_base = lo * expf(-log1pf(t) * M.pinv);
         const float f_brem = 1.f + 1.f / (xterm * M.eta2p1[c] * M.y4p1);
         const float g_brem = 1.f - gpart * M.sqe[c] / M.ep2[c];

@@ -428,6 +428,8 @@ __device__ __forceinline__ double cancel_factor(const double* acc, const float* 
 // Mixed sums whose terms cancel by more than this are recomputed in FP64: the
 // FP32 rounding of each term (a few 1e-7) must stay below 1e-6 in the result.
 constexpr double kMaxCancel = 2.0;
+// FP32 brem cells carry up to ~6e-7 per term (the HR98 fit in FP32).
+constexpr double kMaxCancelBrem = 1.25;
 // The accurate (all-df) pass keeps ~1e-13 per term.
 constexpr double kMaxCancelDf = 1e5;
 
@@ -775,7 +777,7 @@ __global__ void __launch_bounds__(kWarps * 32)
                 acc[kk] = acc[kk] + (double)A.v[kk];
             // cells of both signs (occupation above 1 makes 1 - g negative):
             // recompute this point in FP64
-            redo = cancel_factor(acc, A.mag) > kMaxCancel;
+            redo = cancel_factor(acc, A.mag) > kMaxCancelBrem;
 #pragma unroll
             for (int kk = 0; kk < 16; ++kk)
                 acc[kk] = redo ? 0. : acc[kk] * scale;
@@ -1242,7 +1244,7 @@ enum NesMode
 };
 
 template <int MODE>
-__global__ void __launch_bounds__(kWarps * 32)
+__global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNesAccurate) ? 4 : 1)
     grey_neps_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
                      double* __restrict__ scratch)
 {

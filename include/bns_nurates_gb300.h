@@ -397,6 +397,9 @@ int bnsn_synthetic_points(uint64_t seed, int64_t first, int64_t npts,
  * the FP64-pipe roofline of the opacity kernels.  A diagnostic with no
  * counterpart in the reference. */
 int bnsn_fp64_peak_probe(int64_t iters, double* tflops);
+/* The same for FP32 FMA chains (the pipe of the mixed path's double-float
+ * arithmetic).  A diagnostic with no counterpart in the reference. */
+int bnsn_fp32_peak_probe(int64_t iters, double* tflops);
 
 /* Per-phase device timing of the library's own kernels (diagnostics with no
  * counterpart in the reference).  While enabled, every kernel launch is

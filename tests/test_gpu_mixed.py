@@ -1,0 +1,122 @@
+"""Accuracy of the mixed-precision GPU path against the CPU oracle.
+
+Contract: at most 1e-6 relative error per emissivity and opacity against the
+FP64 oracle, on every output the reference itself computes reproducibly.
+An element's reproducibility is the largest deviation of the oracle under
+three O(eps) perturbations (the FMA build of the same code, and T or mu_e
+moved by two ulps).  Where that deviation is at most 1e-9 the element is well
+conditioned and must be within MIXED_TOL; elsewhere the reference's own
+result moves by more than the mixed path's rounding would explain, and the
+bound is COND_MIXED times that deviation (never below MIXED_TOL).
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+import bns_nurates_gb300 as bn
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+MIXED_TOL = 1e-6
+WELL_CONDITIONED = 1e-9
+COND_MIXED = 1e4
+NTHREADS = os.cpu_count()
+
+
+@pytest.fixture(scope="module")
+def port_fma():
+    import oracle
+    return oracle.port_fma()
+
+
+def _params(pars):
+    return bn.opacity_params(*[bool(v) for v in pars[:5]], brem_implementation=int(pars[5]),
+                             use_NN_medium_corr=bool(pars[6]), neglect_blocking=bool(pars[7]))
+
+
+def _gpu(torch, eos, m1, flags, pars, nq, precision, stim=1, distr=None):
+    q = bn.gauss_legendre(nq)
+    e = torch.from_numpy(np.ascontiguousarray(eos)).cuda()
+    m = torch.from_numpy(np.ascontiguousarray(m1)).cuda()
+    d = None if distr is None else torch.from_numpy(np.ascontiguousarray(distr)).cuda()
+    out = bn.m1_opacities(e, m, bn.opacity_flags(*flags), _params(pars), q, distr=d,
+                          stim_abs=stim, precision=precision)
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def _oracle_with_sens(port, port_fma, eos, m1, flags, pars, nq, stim=1, distr=None):
+    q = port.gauss_legendre(nq)
+    kw = dict(distr=distr, stim_abs=stim, nthreads=NTHREADS)
+    want = port.m1_opacities(eos, m1, flags, pars, q, **kw)
+    sens = rel_err(port_fma.m1_opacities(eos, m1, flags, pars, q, **kw), want, floor=1e-300)
+    for row in (1, 7):
+        e2 = np.array(eos, copy=True)
+        e2[row] *= 1. + 2. ** -51
+        sens = np.maximum(sens, rel_err(port.m1_opacities(e2, m1, flags, pars, q, **kw), want,
+                                        floor=1e-300))
+    return want, sens
+
+
+def _check(got, want, sens, what):
+    assert (np.isfinite(got) == np.isfinite(want)).all(), f"{what}: finiteness differs"
+    r = rel_err(got, want, floor=1e-300)
+    well = sens <= WELL_CONDITIONED
+    assert well.mean() > 0.8, f"{what}: only {well.mean():.2%} of elements well conditioned"
+    worst_well = float(np.max(np.where(well, r, 0.)))
+    assert worst_well <= MIXED_TOL, f"{what}: well-conditioned max rel err {worst_well:.3e}"
+    tol = np.maximum(MIXED_TOL, COND_MIXED * sens)
+    bad = r > tol
+    if bad.any():
+        k = np.unravel_index(np.argmax(r / tol), r.shape)
+        raise AssertionError(f"{what}: {bad.sum()} elements beyond the conditioning bound; "
+                             f"worst {k}: {r[k]:.3e} (sens {sens[k]:.3e})")
+    return worst_well
+
+
+CASES = [
+    # (name, flags, pars, nq, stim)
+    ("all reactions, GP19, n=20", (1, 1, 1, 1, 1), (1, 0, 1, 1, 1, 2, 1, 0), 20, 1),
+    ("all reactions, HR98, n=10", (1, 1, 1, 1, 1), (1, 0, 1, 1, 1, 0, 1, 0), 10, 1),
+    ("beta+iso+pair+HR98, n=10", (1, 1, 1, 0, 1), (1, 0, 1, 1, 1, 0, 1, 0), 10, 1),
+    ("NES only, n=20, not stimulated", (0, 0, 0, 1, 0), (1, 0, 1, 1, 1, 0, 1, 0), 20, 0),
+    ("pair+BRT06, n=8, neglect blocking", (0, 1, 1, 0, 0), (0, 1, 0, 0, 0, 1, 0, 1), 8, 1),
+    ("GP19 brem only, n=12, no medium", (0, 0, 1, 0, 0), (1, 0, 1, 1, 1, 2, 0, 0), 12, 1),
+]
+
+
+@pytest.mark.parametrize("name,flags,pars,nq,stim", CASES, ids=[c[0] for c in CASES])
+def test_mixed_vs_oracle(cuda, port, port_fma, name, flags, pars, nq, stim):
+    eos, m1 = bn.synthetic_points(20261203, 3072, first=777)
+    got = _gpu(cuda, eos, m1, flags, pars, nq, "mixed", stim=stim)
+    want, sens = _oracle_with_sens(port, port_fma, eos, m1, flags, pars, nq, stim=stim)
+    _check(got, want, sens, name)
+
+
+def test_mixed_given_distribution(cuda, port, port_fma):
+    """Given NuDistributionParams, including species whose reconstructed
+    occupation leaves the FP32 range envelope (they take the FP64 pass)."""
+    eos, m1 = bn.synthetic_points(99, 1024)
+    distr = port.distr_from_m1(eos, m1)
+    distr[8 + 2, ::7] = -75.0   # eta_t of nu_x far below the FP32-safe range
+    flags, pars = (1, 1, 1, 1, 1), (1, 0, 1, 1, 1, 0, 1, 0)
+    got = _gpu(cuda, eos, m1, flags, pars, 10, "mixed", distr=distr)
+    want, sens = _oracle_with_sens(port, port_fma, eos, m1, flags, pars, 10, distr=distr)
+    _check(got, want, sens, "given distribution")
+
+
+def test_mixed_close_to_fp64_gpu_and_deterministic(cuda):
+    """Bulk statistics on a larger batch (no oracle): p99.9 of the mixed-vs-FP64
+    deviation below 1e-6; two mixed calls are bitwise identical."""
+    eos, m1 = bn.synthetic_points(5, 65536, first=10 ** 6)
+    flags, pars = (1, 1, 1, 1, 1), (1, 0, 1, 1, 1, 2, 1, 0)
+    a = _gpu(cuda, eos, m1, flags, pars, 20, "mixed")
+    b = _gpu(cuda, eos, m1, flags, pars, 20, "mixed")
+    c = _gpu(cuda, eos, m1, flags, pars, 20, "fp64")
+    assert np.array_equal(a, b)
+    r = rel_err(a, c, floor=1e-300)
+    assert np.percentile(r, 99.9) < MIXED_TOL
+    assert np.isfinite(a).all() == np.isfinite(c).all()
