@@ -410,16 +410,20 @@ struct Acc32
     }
 };
 
-// Largest cancellation factor sum|t| / |sum t| of the number moments of a
-// point (warp-reduced; 1 when every term has one sign).
-__device__ __forceinline__ double cancel_factor(const double* acc, const float* mag)
+// Largest error amplification of the number moments of a point: the sum of
+// |term| over |total|, where the total adds the other reactions' sums of the
+// same output (`other`, already in the units of scale x acc; nullptr: none).
+// Terms are those of this lane (acc, mag, unscaled); the result is
+// warp-reduced and 1 when every contribution has one sign.
+__device__ __forceinline__ double cancel_factor(const double* acc, const float* mag, double scale,
+                                                const double* other)
 {
     double amp = 1.;
 #pragma unroll
     for (int s = 0; s < 8; ++s)
     {
-        const double m   = warp_sum((double)mag[s]);
-        const double tot = fabs(warp_sum(acc[s]));
+        const double m   = warp_sum((double)mag[s]) * scale;
+        const double tot = fabs(warp_sum(acc[s]) * scale + (other ? other[s] : 0.));
         amp = fmax(amp, m > 0. ? m / tot : 1.);
     }
     return amp;
@@ -666,15 +670,8 @@ __global__ void __launch_bounds__(kWarps * 32)
         // Mixed cells in FP32 except BRT06, the GP19 high-T extrapolation and
         // points whose pair sums are negative somewhere: there the outputs
         // (pair + brem + ...) cancel and would magnify FP32 rounding.
-        bool pair_pos = true;
-        if (MIXED && add)
-        {
-            const double v = lane < 16 ? P->s2d[lane] : 0.;
-            pair_pos = __all_sync(0xffffffffu, !(v < 0.));
-        }
         const bool fp32_cells =
-            MIXED && pair_pos &&
-            (IMPL == 0 || (IMPL == 2 && prof && GW.pt.regime != 3 && GW.pt.regime != 5));
+            MIXED && (IMPL == 0 || (IMPL == 2 && prof && GW.pt.regime != 3 && GW.pt.regime != 5));
         double acc[16];
 #pragma unroll
         for (int kk = 0; kk < 16; ++kk)
@@ -775,9 +772,13 @@ __global__ void __launch_bounds__(kWarps * 32)
 #pragma unroll
             for (int kk = 0; kk < 16; ++kk)
                 acc[kk] = acc[kk] + (double)A.v[kk];
-            // cells of both signs (occupation above 1 makes 1 - g negative):
-            // recompute this point in FP64
-            redo = cancel_factor(acc, A.mag) > kMaxCancelBrem;
+            // cells of both signs (occupation above 1 makes 1 - g negative), or
+            // a brem sum cancelling the pair sum: recompute this point in FP64
+            double pair_n[8];
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk)
+                pair_n[kk] = add ? P->s2d[kk] : 0.;
+            redo = cancel_factor(acc, A.mag, scale, pair_n) > kMaxCancelBrem;
 #pragma unroll
             for (int kk = 0; kk < 16; ++kk)
                 acc[kk] = redo ? 0. : acc[kk] * scale;
@@ -1319,13 +1320,6 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
                 }
                 if (!ok)
                     flag = 2;
-                else if (L.use_pair || L.use_brem)
-                {
-                    // negative pair (+ brem) sums: the outputs cancel
-                    const double v = lane < 16 ? P->s2d[lane] : 0.;
-                    if (!__all_sync(0xffffffffu, !(v < 0.)))
-                        flag = 1;
-                }
             }
             if (flag == 0)
             {
@@ -1465,12 +1459,18 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
 #pragma unroll
                 for (int kk = 0; kk < 16; ++kk)
                     acc[kk] = dfm::to_double(dacc[kk]);
-                // terms of both signs (occupation above 1): the fast pass hands
-                // the point to the accurate pass, the accurate pass to FP64
-                const double amp = cancel_factor(acc, mag);
+                // terms of both signs (occupation above 1), or NES sums
+                // cancelling the pair + brem sums of the same output (those enter
+                // the assembly with t2d^2 = hn / 8): the fast pass hands the point
+                // to the accurate pass, the accurate pass to FP64
+                const double T4 = (T * T) * (T * T);
+                double other[8];
+#pragma unroll
+                for (int kk = 0; kk < 8; ++kk)
+                    other[kk] = (L.use_pair || L.use_brem) ? 0.125 * P->s2d[kk] : 0.;
+                const double amp = cancel_factor(acc, mag, NP.pre * T4, other);
                 if (amp > (MODE == kNesFast ? kMaxCancel : kMaxCancelDf))
                     flag = MODE == kNesFast ? 1 : 2;
-                const double T4 = (T * T) * (T * T);
 #pragma unroll
                 for (int kk = 0; kk < 16; ++kk)
                     acc[kk] *= NP.pre * T4 * (kk >= 8 ? T : 1.);
