@@ -341,9 +341,15 @@ __constant__ FdiTab kFdiTab = {
       {2522.7839609396783, 3244.5527999477567, 2403.0532924519756, 1176.7202478443275, 397.7596246691212, 91.84661231161838, 13.491911254479298, 1.0, BNSN_Z}}}};
 #undef BNSN_Z
 
-// r[k-1] = F_k(-|y|), k = 1..5 (the unreflected part of fdi_orders; NaN -> 0).
-__device__ __noinline__ void fdi_raw15(df y, df* r)
+// r[k-1] = F_k(-|y|), k = kmin..5 (the unreflected part of fdi_orders; NaN ->
+// 0); entries below kmin are not written.  `tab` is kFdiTab or a copy of it in
+// shared memory (lanes in different regimes read different coefficients: from
+// shared memory that costs at most a bank conflict, from the constant cache a
+// serialised access per distinct address).
+__device__ __noinline__ void fdi_raw15(df y, df* r, int kmin = 1, const FdiTab* tab = nullptr)
 {
+    if (!tab)
+        tab = &kFdiTab;
     const df x = (y.hi > 0.f) ? neg(y) : y;
     if (!(x.hi <= 0.f))
     {
@@ -368,10 +374,10 @@ __device__ __noinline__ void fdi_raw15(df y, df* r)
     }
     // terms of the forms: x < -2: 5 (k = 1), 4 (k = 2..5); else 9, 9, 8, 8, 8
 #pragma unroll 1
-    for (int k = 0; k < 5; ++k)
+    for (int k = kmin - 1; k < 5; ++k)
     {
-        const dfc* cn = kFdiTab.num[reg][k];
-        const dfc* cd = kFdiTab.den[reg][k];
+        const dfc* cn = tab->num[reg][k];
+        const dfc* cd = tab->den[reg][k];
         const int top = reg == 0 ? (k == 0 ? 4 : 3) : (k < 2 ? 8 : 7);
         df pn = mk(cn[top]), pd = mk(cd[top]);
 #pragma unroll 1

@@ -966,15 +966,54 @@ __device__ __forceinline__ float neps_exp_f32(double d, bool neg)
     return (neg ? 1.f : -e) / dn;
 }
 
+// Taylor branches of neps_pair (kernel_nes.hpp:82-132) for w or w' near 0,
+// in FP64: dimensionless r1 = R(w, w'), r2 = R(w', w) of lepton e.  Rare in the
+// item loop, so kept out of line to keep the loop's code small.
+__device__ __noinline__ void neps_taylor(const NepsPoint& P, int e, double w, double wp,
+                                         double x, double y, int sign1, int sign2, double* r1,
+                                         double* r2)
+{
+    const double eta  = e ? P.eta1 : P.eta0;
+    const double* f0e = e ? P.fe1 : P.fe0;
+    const double fd0  = e ? P.fd01 : P.fd00;
+    if (x > eta * 1e-3)
+    {
+        double fx[3];
+        fdi_orders<0, 2>(eta - x, fx);
+        const double f[5] = {fx[2] - f0e[2], fx[1], f0e[1],
+                             fx[0] + y * fermi_distr(0., 1., eta - x) / 6., f0e[0] - y * fd0 / 6.};
+#pragma unroll
+        for (int s = 0; s < 4; ++s)
+        {
+            double b1, b2;
+            neps_couplings(e, s, &b1, &b2);
+            r1[s] = mb_int_one(x, y, sign1, b1, b2, f);
+            r2[s] = mb_int_one(x, y, sign2, b1, b2, f);
+        }
+    }
+    else
+    {
+        const double f[3] = {fd0, f0e[0], f0e[1]};
+#pragma unroll
+        for (int s = 0; s < 4; ++s)
+        {
+            double b1, b2;
+            neps_couplings(e, s, &b1, &b2);
+            r1[s] = mb_int_two(w, wp, x, y, b1, b2, f);
+            r2[s] = mb_int_two(wp, w, x, y, b1, b2, f);
+        }
+    }
+}
+
 // One item of the mixed path: dimensionless kernels r1 = R(nu, nub) / pre,
 // r2 = R(nub, nu) / pre summed over e- and e+ with NEPSExpFunc applied
 // (em1, ab1, em2, ab2 per species).  The Fermi integrals and the
 // Mezzacappa-Bruenn brackets (kernel_nes.hpp:50-132) run in df: they cancel
 // catastrophically.  The branch structure of neps_pair is kept; the Taylor
 // branches near w, w' -> 0 run in FP64.
-__device__ __forceinline__ void neps_item_mixed(const NepsPoint& P, const NepsMixed& Q, double w,
-                                                double wp, float* em1, float* ab1, float* em2,
-                                                float* ab2)
+__device__ __forceinline__ void neps_item_mixed(const NepsPoint& P, const NepsMixed& Q,
+                                                const dfm::FdiTab* ftab, double w, double wp,
+                                                float* em1, float* ab1, float* em2, float* ab2)
 {
     using namespace dfm;
     const double x = (w > wp) ? w : wp;
@@ -994,8 +1033,10 @@ __device__ __forceinline__ void neps_item_mixed(const NepsPoint& P, const NepsMi
     const df Pp = mul(W, WP);
     const df Dn = mul(Pp, Pp);
     const df X  = from_double(x), Y = from_double(y);
+    // e+ terms scale as e^{-eta_e}: below 1e-13 of the e- terms for eta_e > 30
+    const int nlep = P.eta0 > 30. ? 1 : 2;
 #pragma unroll 1
-    for (int e = 0; e < 2; ++e)
+    for (int e = 0; e < nlep; ++e)
     {
         const double eta = e ? P.eta1 : P.eta0;
         float r1[4], r2[4];
@@ -1008,9 +1049,10 @@ __device__ __forceinline__ void neps_item_mixed(const NepsPoint& P, const NepsMi
             const double adw = fabs(w - wp);
             const df aab = from_double(eta - adw);
             df rw[5], rwp[5], rab[5];
-            fdi_raw15(aw, rw);
-            fdi_raw15(awp, rwp);
-            fdi_raw15(aab, rab);
+            fdi_raw15(aw, rw, 1, ftab);
+            fdi_raw15(awp, rwp, 1, ftab);
+            fdi_raw15(aab, rab, 3, ftab); // only F_3..F_5 enter through |w - w'|
+            rab[0] = rab[1] = Q.reta[e][0]; // unused orders: keep the arrays defined
             df dw[5], d5[5];
             fdi_diff15(rw, rwp, aw, awp, from_double(w - wp), dw);
             fdi_diff15(rab, Q.reta[e], aab, Q.eta[e], from_double(adw), d5);
@@ -1046,35 +1088,13 @@ __device__ __forceinline__ void neps_item_mixed(const NepsPoint& P, const NepsMi
         }
         else
         {
-            const double* f0e = e ? P.fe1 : P.fe0;
-            const double fd0  = e ? P.fd01 : P.fd00;
-            if (x > eta * 1e-3)
-            {
-                double fx[3];
-                fdi_orders<0, 2>(eta - x, fx);
-                const double f[5] = {fx[2] - f0e[2], fx[1], f0e[1],
-                                     fx[0] + y * fermi_distr(0., 1., eta - x) / 6.,
-                                     f0e[0] - y * fd0 / 6.};
+            double t1[4], t2[4];
+            neps_taylor(P, e, w, wp, x, y, (int)sign1, (int)sign2, t1, t2);
 #pragma unroll
-                for (int s = 0; s < 4; ++s)
-                {
-                    double b1, b2;
-                    neps_couplings(e, s, &b1, &b2);
-                    r1[s] = (float)mb_int_one(x, y, (int)sign1, b1, b2, f);
-                    r2[s] = (float)mb_int_one(x, y, (int)sign2, b1, b2, f);
-                }
-            }
-            else
+            for (int s = 0; s < 4; ++s)
             {
-                const double f[3] = {fd0, f0e[0], f0e[1]};
-#pragma unroll
-                for (int s = 0; s < 4; ++s)
-                {
-                    double b1, b2;
-                    neps_couplings(e, s, &b1, &b2);
-                    r1[s] = (float)mb_int_two(w, wp, x, y, b1, b2, f);
-                    r2[s] = (float)mb_int_two(wp, w, x, y, b1, b2, f);
-                }
+                r1[s] = (float)t1[s];
+                r2[s] = (float)t2[s];
             }
         }
 #pragma unroll
@@ -1122,8 +1142,9 @@ __device__ __forceinline__ dfm::df neps_exp_df(double d, bool negd)
 }
 
 // neps_item_mixed with every product after the Fermi integrals in df.
-__device__ __forceinline__ void neps_item_df(const NepsPoint& P, const NepsMixed& Q, double w,
-                                             double wp, dfm::df* em1, dfm::df* ab1, dfm::df* em2,
+__device__ __forceinline__ void neps_item_df(const NepsPoint& P, const NepsMixed& Q,
+                                             const dfm::FdiTab* ftab, double w, double wp,
+                                             dfm::df* em1, dfm::df* ab1, dfm::df* em2,
                                              dfm::df* ab2)
 {
     using namespace dfm;
@@ -1143,8 +1164,10 @@ __device__ __forceinline__ void neps_item_df(const NepsPoint& P, const NepsMixed
     const df Pp = mul(W, WP);
     const df Dn = mul(Pp, Pp);
     const df X  = from_double(x), Y = from_double(y);
+    // e+ terms scale as e^{-eta_e}: below 1e-13 of the e- terms for eta_e > 30
+    const int nlep = P.eta0 > 30. ? 1 : 2;
 #pragma unroll 1
-    for (int e = 0; e < 2; ++e)
+    for (int e = 0; e < nlep; ++e)
     {
         const double eta = e ? P.eta1 : P.eta0;
         df r1[4], r2[4];
@@ -1154,9 +1177,10 @@ __device__ __forceinline__ void neps_item_df(const NepsPoint& P, const NepsMixed
             const double adw = fabs(w - wp);
             const df aab = from_double(eta - adw);
             df rw[5], rwp[5], rab[5];
-            fdi_raw15(aw, rw);
-            fdi_raw15(awp, rwp);
-            fdi_raw15(aab, rab);
+            fdi_raw15(aw, rw, 1, ftab);
+            fdi_raw15(awp, rwp, 1, ftab);
+            fdi_raw15(aab, rab, 3, ftab); // only F_3..F_5 enter through |w - w'|
+            rab[0] = rab[1] = Q.reta[e][0]; // unused orders: keep the arrays defined
             df dw[5], d5[5];
             fdi_diff15(rw, rwp, aw, awp, from_double(w - wp), dw);
             fdi_diff15(rab, Q.reta[e], aab, Q.eta[e], from_double(adw), d5);
@@ -1186,35 +1210,13 @@ __device__ __forceinline__ void neps_item_df(const NepsPoint& P, const NepsMixed
         }
         else
         {
-            const double* f0e = e ? P.fe1 : P.fe0;
-            const double fd0  = e ? P.fd01 : P.fd00;
-            if (x > eta * 1e-3)
-            {
-                double fx[3];
-                fdi_orders<0, 2>(eta - x, fx);
-                const double f[5] = {fx[2] - f0e[2], fx[1], f0e[1],
-                                     fx[0] + y * fermi_distr(0., 1., eta - x) / 6.,
-                                     f0e[0] - y * fd0 / 6.};
+            double t1[4], t2[4];
+            neps_taylor(P, e, w, wp, x, y, (int)sign1, (int)sign2, t1, t2);
 #pragma unroll
-                for (int s = 0; s < 4; ++s)
-                {
-                    double b1, b2;
-                    neps_couplings(e, s, &b1, &b2);
-                    r1[s] = from_double(mb_int_one(x, y, (int)sign1, b1, b2, f));
-                    r2[s] = from_double(mb_int_one(x, y, (int)sign2, b1, b2, f));
-                }
-            }
-            else
+            for (int s = 0; s < 4; ++s)
             {
-                const double f[3] = {fd0, f0e[0], f0e[1]};
-#pragma unroll
-                for (int s = 0; s < 4; ++s)
-                {
-                    double b1, b2;
-                    neps_couplings(e, s, &b1, &b2);
-                    r1[s] = from_double(mb_int_two(w, wp, x, y, b1, b2, f));
-                    r2[s] = from_double(mb_int_two(wp, w, x, y, b1, b2, f));
-                }
+                r1[s] = from_double(t1[s]);
+                r2[s] = from_double(t2[s]);
             }
         }
 #pragma unroll
@@ -1253,6 +1255,7 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
     __shared__ double s_x2[kMaxQ], s_w2[kMaxQ], s_wx[kMaxQ], s_wx3[kMaxQ];
     __shared__ NepsTab s_nt[kWarps];
     __shared__ NepsMixed s_nm[MIX ? kWarps : 1];
+    __shared__ dfm::FdiTab s_ftab;
     for (int k = threadIdx.x; k < kMaxQ; k += blockDim.x)
     {
         s_x2[k]  = L.x2[k];
@@ -1260,6 +1263,9 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
         s_wx[k]  = L.wx[k];
         s_wx3[k] = L.wx3[k];
     }
+    if (MIX)
+        for (int k = threadIdx.x; k < (int)(sizeof(dfm::FdiTab) / sizeof(float)); k += blockDim.x)
+            ((float*)&s_ftab)[k] = ((const float*)&dfm::kFdiTab)[k];
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int wid  = threadIdx.x >> 5;
@@ -1327,7 +1333,7 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
                 if (lane < 2)
                 {
                     Q.eta[lane] = dfm::from_double(lane ? NP.eta1 : NP.eta0);
-                    dfm::fdi_raw15(Q.eta[lane], Q.reta[lane]);
+                    dfm::fdi_raw15(Q.eta[lane], Q.reta[lane], 1, &s_ftab);
                 }
                 else if (lane >= 8 && lane < 12)
                 {
@@ -1369,7 +1375,7 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
                     if (MODE == kNesFast)
                     {
                         float em1[4], ab1[4], em2[4], ab2[4];
-                        neps_item_mixed(NP, Q, w, wp, em1, ab1, em2, ab2);
+                        neps_item_mixed(NP, Q, &s_ftab, w, wp, em1, ab1, em2, ab2);
                         float g[4], gm[4], gb[4], gbm[4];
                         total_nu_f32(nu, lnu, Q, g, gm);
                         total_nu_f32(nub, lnub, Q, gb, gbm);
@@ -1411,7 +1417,7 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
                     {
                         using namespace dfm;
                         df em1[4], ab1[4], em2[4], ab2[4];
-                        neps_item_df(NP, Q, w, wp, em1, ab1, em2, ab2);
+                        neps_item_df(NP, Q, &s_ftab, w, wp, em1, ab1, em2, ab2);
                         double wt[4], wfd[4];
 #pragma unroll
                         for (int s = 0; s < 4; ++s)
