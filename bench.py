@@ -58,6 +58,11 @@ WORKLOADS = {
                desc="128^3 = 2,097,152 points, beta+iso+pair+HR98, n=10"),
     "c3": dict(npts=128 ** 3, flags=(1, 1, 1, 0, 1), brem=0, nq=10,
                desc="128^3 = 2,097,152 points, beta+iso+pair+HR98, n=10"),
+    "c4": dict(npts=0, flags=None, brem=None, nq=None,
+               desc="1536 AMR blocks, edges {8,16,24,32,48,64} (weights .55/.28/.09/.05/.025/"
+                    ".005, ~12.9M points), per block: brem HR98/BRT06/GP19, NES on/off, n=10 "
+                    "(rho<1e11) or 20; one step = one replay of the CUDA graph of the tuned "
+                    "plan over all blocks"),
     "c5": dict(npts=256 * 256 * 16, flags=(1, 1, 1, 1, 1), brem=2, nq=20,
                desc="256^3 all reactions (beta+WM+mean field, iso, pair, GP19 brem, NES/NPS), "
                     "n=20; one step = one 256x256x16 slab = 1,048,576 points"),
@@ -188,6 +193,9 @@ def run_reference(args, rank, world):
     libbuild.build()
     wl = dict(WORKLOADS[args.workload])
     nthreads = os.cpu_count()
+    if args.workload == "c4":
+        run_reference_blocks(args, wl, nthreads)
+        return
     cap = min(wl["npts"], 1 << 18)
     eos, m1 = bn.synthetic_points(SEED, cap)
     per_step = max(2.0, min(args.cpu_seconds, 150.0 / max(1, args.steps + args.warmup)))
@@ -213,6 +221,54 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
+def run_reference_blocks(args, wl, nthreads):
+    """Reference algorithm on the host cores for the AMR-block workload: the
+    oracle per block (its reactions, brem and n) over the leading blocks, up to
+    about --cpu-seconds of work per step."""
+    import oracle
+    import bns_nurates_gb300 as bn
+    blocks, n = c4_blocks(SEED, 1536, None)
+    cap = min(n, 1 << 17)
+    eos, m1 = bn.synthetic_points(SEED, cap)
+    rho = eos[0] * 1.66053906892e-24 * 1e21
+    port = oracle.port()
+
+    def sample(npts):
+        done, t0 = 0, time.perf_counter()
+        for first, count, flags, brem, _ in blocks:
+            if first + count > cap or done >= npts:
+                break
+            nq = 10 if rho[first] < 1e11 else 20
+            sl = slice(first, first + count)
+            port.m1_opacities(np.ascontiguousarray(eos[:, sl]), np.ascontiguousarray(m1[:, sl]),
+                              flags, (1, 0, 1, 1, 1, brem, 1, 0), port.gauss_legendre(nq),
+                              nthreads=nthreads)
+            done += count
+        return done, time.perf_counter() - t0
+
+    d, dt = sample(4096)
+    target = max(1024, int(d / dt * max(2.0, min(args.cpu_seconds, 150.0 /
+                                                   max(1, args.steps + args.warmup)))))
+    for _ in range(args.warmup):
+        sample(1024)
+    rates = []
+    for _ in range(args.steps):
+        d, dt = sample(target)
+        rates.append(d / dt)
+    value = statistics.median(rates)
+    print(json.dumps({
+        "impl": "reference", "metric": "grey M1 opacity points/s", "value": value,
+        "unit": "points/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * d / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+        "config": {"workload": wl["desc"], "sample": f"leading blocks, ~{target} points per step",
+                   "precision": "fp64 (reference CPU algorithm)"},
+        "cpu_baseline": {"value": value, "unit": "points/s", "cores": nthreads, "kind": "port",
+                         "sample": f"leading blocks of the AMR workload, ~{target} points"},
+        "e2e": {"value": value, "unit": "points/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0}}))
+
+
 def rel_err(a, b):
     """|a - b| / |b| elementwise, 0 where both are equal (including zeros)."""
     with np.errstate(divide="ignore", invalid="ignore"):
@@ -235,11 +291,170 @@ def timed_steps(step, steps, stream, torch):
     return t0.elapsed_time(t1)
 
 
+C4_EDGES = (8, 16, 24, 32, 48, 64)
+C4_WEIGHTS = (0.55, 0.28, 0.09, 0.05, 0.025, 0.005)
+
+
+def c4_blocks(seed, nblocks, eos_first_rho):
+    """Block table of the AMR workload: edge^3 points per block, reactions
+    beta+iso+pair always, brem variant uniform, NES on/off, n by density."""
+    rng = np.random.default_rng(seed)
+    blocks, first = [], 0
+    for _ in range(nblocks):
+        e = int(rng.choice(C4_EDGES, p=C4_WEIGHTS))
+        count = e ** 3
+        brem = int(rng.integers(0, 3))
+        nes = int(rng.integers(0, 2))
+        blocks.append([first, count, (1, 1, 1, nes, 1), brem, None])
+        first += count
+    return blocks, first
+
+
+def run_blocks(args, rank, world, local):
+    """The batched-AMR workload through bnsn_blocks_plan_create / _run in a
+    CUDA graph."""
+    import torch
+    import bns_nurates_gb300 as bn
+    from bns_nurates_gb300 import build as libbuild
+    from bns_nurates_gb300 import shards
+    if rank == 0:
+        libbuild.build()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist.barrier()
+        libbuild.build()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from bns_nurates_gb300 import gp19_synthetic
+    bn.set_gp19_table(gp19_synthetic.table())
+    blocks, n = c4_blocks(SEED + rank, 1536, None)
+    if args.npts:   # smaller runs: keep the first blocks up to npts points
+        keep, tot = [], 0
+        for b in blocks:
+            if tot + b[1] > args.npts:
+                break
+            keep.append(b)
+            tot += b[1]
+        blocks, n = keep, tot
+    first, _ = shards.rank_points(n, rank)
+    t0 = time.perf_counter()
+    eos_h, m1_h = bn.synthetic_points(SEED, n, first=first)
+    gen_s = time.perf_counter() - t0
+    rho = eos_h[0] * 1.66053906892e-24 * 1e21   # nb [nm^-3] -> rho [g cm^-3]
+    for b in blocks:
+        b[4] = 10 if rho[b[0]] < 1e11 else 20
+    eos = torch.from_numpy(eos_h).to(dev)
+    m1 = torch.from_numpy(m1_h).to(dev)
+    out = torch.empty((20, n), dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(dev)
+    warmup = max(args.warmup, 3)
+    plans, graphs, outs, tune_s = {}, {}, {}, {}
+    precs = [args.precision] + (["fp64"] if args.precision == "mixed" and not args.no_fp64 else [])
+    for prec in precs:
+        o = out if prec == args.precision else torch.empty_like(out)
+        t0 = time.perf_counter()
+        plans[prec] = bn.BlocksPlan(blocks, eos, m1, o, precision=prec, tune=True, stream=stream)
+        torch.cuda.synchronize()
+        tune_s[prec] = time.perf_counter() - t0
+        with torch.cuda.stream(stream):
+            plans[prec].run(eos, m1, o, stream=stream)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        l0 = bn.kernel_launches()
+        with torch.cuda.graph(g, stream=stream):
+            plans[prec].run(eos, m1, o, stream=stream)
+        per_replay = bn.kernel_launches() - l0   # library kernels captured in the graph
+        graphs[prec], outs[prec] = g, o
+        if prec == args.precision:
+            launches_per_step = per_replay
+
+    def timed(prec, steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        with torch.cuda.stream(stream):
+            for _ in range(steps):
+                graphs[prec].replay()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    for _ in range(warmup):
+        timed(args.precision, 1)
+    if world > 1:
+        torch.distributed.barrier()
+    with ClockSampler(local) as clk:
+        ms = timed(args.precision, args.steps)
+    ms = shards.max_over_ranks(ms, dev)
+    value = world * n / (ms * 1e-3)
+    res = outs[args.precision].cpu().numpy()
+    fp64 = accuracy = None
+    if "fp64" in graphs and args.precision == "mixed":
+        timed("fp64", 1)
+        ms64 = timed("fp64", 1)
+        fp64 = {"value": world * n / (ms64 * 1e-3), "unit": "points/s", "ms_per_step": ms64,
+                "steps": 1, "warmup": 1, "mixed_over_fp64": ms64 / ms}
+        r = rel_err(res, outs["fp64"].cpu().numpy())
+        accuracy = {"vs": "plain FP64 GPU path (same plan, FP64), every output of every point",
+                    "max_rel": float(r.max()), "p99_rel": float(np.percentile(r, 99)),
+                    "p999_rel": float(np.percentile(r, 99.9)),
+                    "frac_above_1e-6": float(np.mean(r > 1e-6))}
+    # end to end: pinned host inputs -> device, graph replay, outputs -> host
+    e2e = None
+    if not args.no_e2e:
+        eos_p = torch.from_numpy(eos_h).pin_memory()
+        m1_p = torch.from_numpy(m1_h).pin_memory()
+        out_p = torch.empty((20, n), dtype=torch.float64).pin_memory()
+        ksteps = max(1, min(args.steps, 2))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(ksteps):
+            with torch.cuda.stream(stream):
+                eos.copy_(eos_p, non_blocking=True)
+                m1.copy_(m1_p, non_blocking=True)
+                graphs[args.precision].replay()
+                out_p.copy_(outs[args.precision], non_blocking=True)
+            stream.synchronize()
+        dt = shards.max_over_ranks((time.perf_counter() - t0) / ksteps, dev)
+        e2e = {"value": world * n / dt, "unit": "points/s",
+               "h2d_bytes_per_step": int(23 * 8 * n), "d2h_bytes_per_step": int(20 * 8 * n),
+               "call": "BlocksPlan.run in a CUDA graph with host-buffer copies"}
+    groups = plans[args.precision].groups()
+    if rank == 0:
+        nq20 = sum(1 for b in blocks if b[4] == 20)
+        line = {
+            "metric": "grey M1 opacity points/s, mixed vs FP64 GPU",
+            "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps,
+            "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "data": "synthetic (seeded generator with the reference's input ranges)",
+            "config": {"workload": WORKLOADS["c4"]["desc"], "blocks": len(blocks),
+                       "points_per_step_per_gpu": n, "blocks_n20": nq20,
+                       "precision": args.precision, "groups": len(groups),
+                       "l2": "inputs (%.0f MB per GPU) larger than L2 (129 MB)"
+                             % (23 * 8 * n / 1e6),
+                       "parallelism": f"{world} independent point shards"},
+            "fp64_gpu": fp64, "accuracy": accuracy, "e2e": e2e,
+            "autotuner": {"plan_create_s": tune_s, "groups": groups},
+            "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps,
+            "generator_s": gen_s,
+        }
+        print(json.dumps(line))
+    for p_ in plans.values():
+        p_.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "c4":
+        run_blocks(args, rank, world, local)
         return
 
     import torch

@@ -8,7 +8,7 @@ is the Python host mirror of its C ABI (``include/bns_nurates_gb300.h``).
 from ._capi import (BREM_BRT06, BREM_GP19, BREM_HR98, FP64, MIXED,  # noqa: F401
                     GreyOpacityParams, M1Opacities, MyEOSParams, MyQuadrature,
                     NuDistributionParams, OpacityFlags, OpacityParams, SpectralOpacities)
-from .api import (BnsnError, ComputeM1Opacities, ComputeM1OpacitiesNotStimulated,  # noqa: F401
+from .api import (BlocksPlan, BnsnError, ComputeM1Opacities, ComputeM1OpacitiesNotStimulated,  # noqa: F401
                   ComputeSpectralOpacitiesNotStimulatedAbs,
                   ComputeSpectralOpacitiesStimulatedAbs, distr_from_m1, flags_tuple,
                   fp32_peak_tflops, fp64_peak_tflops, gauss_legendre, kernel_launches, m1_opacities,

@@ -105,6 +105,11 @@ class SpectralOpacities(ctypes.Structure):
 P = ctypes.c_void_p
 
 
+class Block(ctypes.Structure):
+    _fields_ = [("first", ctypes.c_int64), ("count", ctypes.c_int64), ("flags", OpacityFlags),
+                ("brem_implementation", c_int), ("nquad", c_int)]
+
+
 class EosSoA(ctypes.Structure):
     _fields_ = [(n, P) for n in ("nb", "temp", "ye", "yp", "yn", "mu_p", "mu_n", "mu_e",
                                   "mu_mu", "dU", "dm_eff")]
@@ -142,6 +147,11 @@ SIGNATURES = {
     "bnsn_gauss_legendre": (c_int, [P]),
     "bnsn_synthetic_points": (c_int, [ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64, P, P,
                                       c_int]),
+    "bnsn_blocks_plan_create": (c_int, [P, c_int, P, c_int, c_int, c_int, P, P, P, P, P]),
+    "bnsn_blocks_run": (c_int, [P, P, P, P, P]),
+    "bnsn_blocks_plan_groups": (c_int, [P]),
+    "bnsn_blocks_plan_info": (c_int, [P, c_int, P, P, P, P, P, P]),
+    "bnsn_blocks_plan_destroy": (c_int, [P]),
     "bnsn_fp64_peak_probe": (c_int, [ctypes.c_int64, P]),
     "bnsn_fp32_peak_probe": (c_int, [ctypes.c_int64, P]),
     "bnsn_phase_timing": (c_int, [c_int]),

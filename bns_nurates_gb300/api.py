@@ -304,3 +304,58 @@ def ComputeSpectralOpacitiesNotStimulatedAbs(nu, quad_1d, grey_pars):
     _check(C.load().bnsn_compute_spectral_opacities_point(
         float(nu), ctypes.byref(quad_1d), ctypes.byref(grey_pars), 0, ctypes.byref(o)))
     return _struct_dict(o)
+
+
+# ---------------------------------------------------------------------------
+# batched AMR blocks
+# ---------------------------------------------------------------------------
+
+class BlocksPlan:
+    """Planned grey opacities of many AMR blocks (bnsn_blocks_plan_create /
+    bnsn_blocks_run).  `blocks` is a sequence of (first, count, flags, brem,
+    nquad) with flags a 5-tuple (abs_em, pair, brem, inelastic, iso); eos [11,
+    N], m1 [12, N] and out [20, N] are CUDA tensors holding every block's
+    points."""
+
+    def __init__(self, blocks, eos, m1, out, params=None, stim_abs=1, precision="fp64",
+                 tune=False, stream=None):
+        lib = C.load()
+        arr = (C.Block * max(1, len(blocks)))()
+        for k, (first, count, flags, brem, nq) in enumerate(blocks):
+            arr[k] = C.Block(int(first), int(count), opacity_flags(*flags), int(brem), int(nq))
+        self._handle = ctypes.c_void_p()
+        params = opacity_params() if params is None else params
+        _check(lib.bnsn_blocks_plan_create(
+            arr, len(blocks), ctypes.byref(params), int(stim_abs), _prec(precision), int(bool(tune)),
+            ctypes.byref(_eos_soa(eos)), ctypes.byref(_m1_soa(m1)), ctypes.byref(_grey_soa(out)),
+            _stream_handle(stream), ctypes.byref(self._handle)))
+
+    def run(self, eos, m1, out, stream=None):
+        _check(C.load().bnsn_blocks_run(self._handle, ctypes.byref(_eos_soa(eos)),
+                                        ctypes.byref(_m1_soa(m1)), ctypes.byref(_grey_soa(out)),
+                                        _stream_handle(stream)))
+        return out
+
+    def groups(self):
+        lib = C.load()
+        res = []
+        for g in range(lib.bnsn_blocks_plan_groups(self._handle)):
+            nq, rx, br = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+            n, ch, gs = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double()
+            _check(lib.bnsn_blocks_plan_info(self._handle, g, ctypes.byref(nq), ctypes.byref(rx),
+                                             ctypes.byref(br), ctypes.byref(n), ctypes.byref(ch),
+                                             ctypes.byref(gs)))
+            res.append(dict(nquad=nq.value, reactions=rx.value, brem=br.value, npts=n.value,
+                            chunk=ch.value, grid_scale=gs.value))
+        return res
+
+    def close(self):
+        if self._handle:
+            C.load().bnsn_blocks_plan_destroy(self._handle)
+            self._handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -21,6 +21,8 @@ struct Gp19Dev
 struct OpacityLaunch
 {
     int64_t npts;
+    const int64_t* pidx;   // point q of the launch is pidx[q] (NULL: q itself)
+    double grid_scale;     // persistent grid = grid_scale x resident CTAs (0: 1)
     const double* eos[11]; // nb temp ye yp yn mu_p mu_n mu_e mu_mu dU dm_eff
     const double* m1[12];  // n[4] J[4] chi[4]
     const double* distr[28];
@@ -72,6 +74,19 @@ void phase_mark(int phase, int end, cudaStream_t stream);
 // scratch records of grey_point_scratch_bytes() (= kGreyRecordBytes) each.
 constexpr size_t kGreyRecordBytes = 767 * sizeof(double);
 size_t grey_point_scratch_bytes();
+
+// C-ABI helpers shared by the entry-point translation units (capi.cu).
+struct DeviceInfo
+{
+    int num_sms;
+    Gp19Dev gp19;
+    bool has_gp19;
+};
+int capi_fail(int code, const char* msg);              // records the message, returns code
+int capi_cuda_fail(cudaError_t e, const char* where);
+int capi_fill_launch(const void* quad_1d, const void* quad_2d, const void* flags,
+                     const void* params, int stim, OpacityLaunch* L); // MyQuadrature etc.
+int capi_device_info(DeviceInfo* info);                // current device (creates its state)
 
 // Static scratch of bnsn_m1_opacities_noalloc: room for kNoAllocPoints grey
 // records in a file-scope __device__ array.  noalloc_scratch() looks up its

@@ -264,6 +264,26 @@ int attach_device(OpacityLaunch* L, DeviceState** st)
 
 } // namespace
 
+int bnsn::capi_fail(int code, const char* msg) { return fail(code, msg); }
+int bnsn::capi_cuda_fail(cudaError_t e, const char* where) { return cuda_fail(e, where); }
+int bnsn::capi_fill_launch(const void* q1, const void* q2, const void* fl, const void* pa,
+                           int stim, OpacityLaunch* L)
+{
+    return fill_common((const MyQuadrature*)q1, (const MyQuadrature*)q2, (const OpacityFlags*)fl,
+                       (const OpacityParams*)pa, stim, L);
+}
+int bnsn::capi_device_info(DeviceInfo* info)
+{
+    DeviceState* st;
+    const int rc = device_state(&st);
+    if (rc)
+        return rc;
+    info->num_sms  = st->num_sms;
+    info->gp19     = st->g;
+    info->has_gp19 = st->gp19;
+    return BNSN_OK;
+}
+
 // ---------------------------------------------------------------------------
 // phase timing and launch counting
 // ---------------------------------------------------------------------------

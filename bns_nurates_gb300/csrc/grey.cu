@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kWarps * 32)
 
     for (int64_t q = (int64_t)blockIdx.x * kWarps + (threadIdx.x >> 5); q < np; q += nwarp)
     {
-        const int64_t p = p0 + q;
+        const int64_t p = L.pidx ? L.pidx[p0 + q] : p0 + q;
         const double nb = L.eos[0][p], T = L.eos[1][p];
         const double yp = L.eos[3][p], yn = L.eos[4][p];
         const double mu_e = L.eos[7][p];
@@ -517,7 +517,7 @@ __global__ void __launch_bounds__(kWarps * 32)
 
     for (int64_t q = (int64_t)blockIdx.x * kWarps + wid; q < np; q += nwarp)
     {
-        const int64_t p  = p0 + q;
+        const int64_t p  = L.pidx ? L.pidx[p0 + q] : p0 + q;
         PointTab* P      = (PointTab*)(scratch + q * kTabWords);
         const double T   = L.eos[1][p];
         const double eta = L.eos[7][p] / T;
@@ -640,7 +640,7 @@ __global__ void __launch_bounds__(kWarps * 32)
 
     for (int64_t q = (int64_t)blockIdx.x * kWarps + wid; q < np; q += nwarp)
     {
-        const int64_t p = p0 + q;
+        const int64_t p = L.pidx ? L.pidx[p0 + q] : p0 + q;
         PointTab* P     = (PointTab*)(scratch + q * kTabWords);
         const double T  = L.eos[1][p];
         __syncwarp();
@@ -1276,7 +1276,7 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
 
     for (int64_t q = (int64_t)blockIdx.x * kWarps + wid; q < np; q += nwarp)
     {
-        const int64_t p = p0 + q;
+        const int64_t p = L.pidx ? L.pidx[p0 + q] : p0 + q;
         PointTab* P     = (PointTab*)(scratch + q * kTabWords);
         if (MODE == kNesAccurate && P->neps_fp64 != 1.)
             continue;
@@ -1511,7 +1511,7 @@ __global__ void __launch_bounds__(128)
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < np;
          q += (int64_t)gridDim.x * blockDim.x)
     {
-        const int64_t p     = p0 + q;
+        const int64_t p     = L.pidx ? L.pidx[p0 + q] : p0 + q;
         const PointTab* P   = (const PointTab*)(scratch + q * kTabWords);
         const double T      = L.eos[1][p];
         const double eta_e  = L.eos[7][p] / T;
@@ -1578,6 +1578,10 @@ __global__ void __launch_bounds__(128)
     }
 }
 
+// Persistent grid: resident CTAs (occupancy) x num_sms x the launch's
+// grid_scale (a tuning knob; 1 by default), capped by the work.
+thread_local double g_grid_scale = 1.;
+
 template <class K>
 int grid_for(K kernel, int threads, int64_t work, int num_sms)
 {
@@ -1586,7 +1590,8 @@ int grid_for(K kernel, int threads, int64_t work, int num_sms)
             cudaSuccess ||
         per_sm < 1)
         per_sm = 1;
-    const int64_t cap = (int64_t)num_sms * per_sm;
+    int64_t cap = (int64_t)((double)num_sms * per_sm * g_grid_scale);
+    cap = cap < 1 ? 1 : cap;
     return (int)(work < cap ? (work > 0 ? work : 1) : cap);
 }
 
@@ -1621,6 +1626,7 @@ cudaError_t launch_grey(const OpacityLaunch& L, cudaStream_t st, int sms, double
         return cudaSuccess;
     if (!ws || ws_points < 1)
         return cudaErrorInvalidValue;
+    g_grid_scale = L.grid_scale > 0. ? L.grid_scale : 1.;
     for (int64_t p0 = 0; p0 < L.npts; p0 += ws_points)
     {
         const int64_t np = (L.npts - p0) < ws_points ? (L.npts - p0) : ws_points;

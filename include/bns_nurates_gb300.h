@@ -310,6 +310,49 @@ int bnsn_m1_opacities_noalloc(const MyQuadrature* quad_1d, const MyQuadrature* q
                               int precision, const bnsn_m1_opacities_soa* out,
                               int64_t npts, void* stream);
 
+/* ----------------------------------------------------------------------
+ * Batched AMR blocks (no counterpart in the reference, whose callers loop
+ * over points): many blocks of uneven size, each with its own reactions,
+ * bremsstrahlung variant and quadrature order, computed by one planned
+ * execution.  A block is points [first, first + count) of the SoA arrays.
+ * ---------------------------------------------------------------------- */
+typedef struct bnsn_block
+{
+    int64_t first;
+    int64_t count;
+    OpacityFlags flags;      /* reactions of the block */
+    int brem_implementation; /* BremImpl of the block */
+    int nquad;               /* Gauss-Legendre nodes per half-interval (1d and 2d) */
+} bnsn_block;
+
+typedef struct bnsn_blocks_plan* bnsn_blocks_plan_t;
+
+/* Plan the blocks: group them by configuration, upload each group's point
+ * list, allocate the per-point scratch, and with tune != 0 time candidate
+ * launch shapes (points per scratch chunk, persistent-grid scale) per group on
+ * the given arrays, keeping the fastest (the tuning runs write `out`).
+ * Allocates device memory and synchronises; the GP19 table, when a block uses
+ * it, must be loaded before and not replaced while the plan lives. */
+int bnsn_blocks_plan_create(const bnsn_block* blocks, int nblocks,
+                            const OpacityParams* params, int stim_abs, int precision,
+                            int tune, const bnsn_eos_soa* eos, const bnsn_m1_soa* m1,
+                            const bnsn_m1_opacities_soa* out, void* stream,
+                            bnsn_blocks_plan_t* plan);
+/* Grey opacities of every block of the plan on `stream`.  Kernel launches
+ * only (no allocation, host synchronisation or copy), so a run can be
+ * captured in a CUDA graph and replayed; the arrays may differ from the ones
+ * given to the plan but must hold the same points. */
+int bnsn_blocks_run(bnsn_blocks_plan_t plan, const bnsn_eos_soa* eos,
+                    const bnsn_m1_soa* m1, const bnsn_m1_opacities_soa* out,
+                    void* stream);
+/* Number of configuration groups, and the configuration, size and chosen
+ * launch shape of group g (reactions: bit 0 abs/em, 1 pair, 2 brem, 3 NES,
+ * 4 iso).  Output pointers may be NULL. */
+int bnsn_blocks_plan_groups(bnsn_blocks_plan_t plan);
+int bnsn_blocks_plan_info(bnsn_blocks_plan_t plan, int group, int* nquad, int* reactions,
+                          int* brem, int64_t* npts, int64_t* chunk, double* grid_scale);
+int bnsn_blocks_plan_destroy(bnsn_blocks_plan_t plan);
+
 /* Spectral opacities of npts points at n_energies neutrino energies
  * (`energies` is a host array, MeV).  Replaces
  * ComputeSpectralOpacitiesStimulatedAbs (stimulated = 1,
