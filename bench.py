@@ -569,9 +569,9 @@ def main():
     bound = c.get("bound", "fp64")
     probe = bn.fp64_peak_tflops if bound == "fp64" else bn.fp32_peak_tflops
     peak = probe()
-    chunks = -(-n // 16384) * args.steps       # launches of the phase: one per scratch chunk
-    pts_per_launch = n * args.steps / max(1, chunks)
-    top_launch_ms = top_ms / max(1, chunks)
+    chunks = max(1, top_launches)                # one launch of the phase per scratch chunk
+    pts_per_launch = n * args.steps / chunks
+    top_launch_ms = top_ms / chunks
     roofline = {"kernel": f"grey phase '{top}'", "bound": bound, "unit": "TFLOP/s",
                 "achieved": None, "peak": peak, "frac": None, "traffic": None,
                 "peak_source": f"{bound.upper()} FMA-chain probe run in this process "

@@ -33,8 +33,8 @@ struct Group
     OpacityLaunch L;      // flags, params, quadrature and weights of the group
     int64_t* pidx = nullptr;
     int64_t npts  = 0;
-    int64_t chunk = 16384; // points per scratch chunk
-    double grid   = 1.;    // persistent-grid scale
+    int64_t chunk = 8192; // points per scratch chunk (untuned default)
+    double grid   = 2.;   // persistent-grid scale (untuned default)
 };
 
 // Candidate launch shapes of the tuner: (points per chunk, grid scale), timed

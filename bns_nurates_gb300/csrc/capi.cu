@@ -56,9 +56,10 @@ struct DeviceState
     cudaMemPool_t pool = nullptr; // grey scratch records
 };
 
-// Points per grey scratch chunk: 16384 records of ~6 KB stay resident in L2
-// between the phase kernels of a chunk.
-constexpr int64_t kGreyChunk = 16384;
+// Points per grey scratch chunk: 8192 records of ~6 KB (50 MB) stay resident
+// in L2 between the phase kernels of a chunk (the batched-blocks autotuner
+// picks this size on most configurations).
+constexpr int64_t kGreyChunk = 8192;
 
 std::mutex g_mu;
 std::map<int, DeviceState> g_dev;

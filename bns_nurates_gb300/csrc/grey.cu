@@ -1579,7 +1579,7 @@ __global__ void __launch_bounds__(128)
 }
 
 // Persistent grid: resident CTAs (occupancy) x num_sms x the launch's
-// grid_scale (a tuning knob; 1 by default), capped by the work.
+// grid_scale (a tuning knob; 2 by default), capped by the work.
 thread_local double g_grid_scale = 1.;
 
 template <class K>
@@ -1626,7 +1626,9 @@ cudaError_t launch_grey(const OpacityLaunch& L, cudaStream_t st, int sms, double
         return cudaSuccess;
     if (!ws || ws_points < 1)
         return cudaErrorInvalidValue;
-    g_grid_scale = L.grid_scale > 0. ? L.grid_scale : 1.;
+    // default: two waves of resident CTAs per phase kernel (per-point work is
+    // uneven; the second wave fills the tail of the first)
+    g_grid_scale = L.grid_scale > 0. ? L.grid_scale : 2.;
     for (int64_t p0 = 0; p0 < L.npts; p0 += ws_points)
     {
         const int64_t np = (L.npts - p0) < ws_points ? (L.npts - p0) : ws_points;

@@ -191,7 +191,7 @@ typedef struct SpectralOpacities
  * not synchronise the host.
  *
  * Device memory: bnsn_m1_opacities keeps a per-point scratch record (about
- * 6 KB) for at most 16384 points at a time.  It takes that scratch from a
+ * 6 KB) for at most 8192 points at a time.  It takes that scratch from a
  * library-owned stream-ordered memory pool (one per device, created on the
  * first call), allocating and freeing it in order on `stream`, so calls on
  * different streams never share scratch.  The pool keeps its memory for
