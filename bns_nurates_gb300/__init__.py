@@ -13,8 +13,8 @@ from .api import (BlocksPlan, BnsnError, ComputeM1Opacities, ComputeM1OpacitiesN
                   ComputeSpectralOpacitiesStimulatedAbs, distr_from_m1, flags_tuple,
                   fp32_peak_tflops, fp64_peak_tflops, gauss_legendre, kernel_launches, m1_opacities,
                   m1_opacities_host, nu_equilibrium, opacity_flags, opacity_params, params_tuple,
-                  phase_times, phase_timing, quad_arrays, set_gp19_table, spectral_opacities,
-                  synthetic_points)
+                  phase_times, phase_timing, quad_arrays, set_gp19_table, spectral_mixed_stats,
+                  spectral_opacities, synthetic_points)
 
 
 def lib():

@@ -255,6 +255,14 @@ def kernel_launches():
     return int(C.load().bnsn_kernel_launches())
 
 
+def spectral_mixed_stats(reset=False):
+    """Mixed spectral path on the current device since the last reset:
+    {"evaluated", "fp64", "pb_fp64", "nes_fp64"} (point, energy) counts."""
+    c = (ctypes.c_int64 * 4)()
+    _check(C.load().bnsn_spectral_mixed_stats(c, int(reset)))
+    return dict(zip(("evaluated", "fp64", "pb_fp64", "nes_fp64"), (int(v) for v in c)))
+
+
 def m1_opacities_host(eos, m1, flags, params, quad_1d, quad_2d=None, stim_abs=1,
                       precision="fp64", out=None):
     """Grey opacities of host (numpy or pinned torch) arrays, copies included."""

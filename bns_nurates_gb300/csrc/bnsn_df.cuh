@@ -24,6 +24,7 @@
 
 namespace bnsn {
 namespace dfm {
+namespace { // internal linkage: every translation unit has its own copy
 
 #define BNSN_DI __device__ __forceinline__
 
@@ -466,5 +467,6 @@ BNSN_DI void fdi_diff15(const df* ra, const df* rb, df a, df b, df delta, df* dw
 
 #undef BNSN_DI
 
+} // namespace
 } // namespace dfm
 } // namespace bnsn

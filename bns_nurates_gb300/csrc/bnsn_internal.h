@@ -42,6 +42,7 @@ struct OpacityLaunch
     double wx[kMaxQ];      // NES: w_i x_i
     double wx3[kMaxQ];     // NES: w_i / x_i^3
     double lx2[kMaxQ], l1m[kMaxQ], l1p[kMaxQ]; // NES: log x_i, log(1 - x_i), log(1 + x_i)
+    double lx1[kMaxQ];     // spectral: log of the 1-D nodes
     uint32_t cells[kMaxCells]; // a | b << 16, a <= b
     Gp19Dev gp19;
     // spectral launches only
@@ -95,7 +96,16 @@ constexpr int64_t kNoAllocPoints = 4096;
 cudaError_t noalloc_scratch(int device, double** ptr);
 cudaError_t launch_grey(const OpacityLaunch& L, cudaStream_t stream, int num_sms, double* ws,
                         int64_t ws_points);
-cudaError_t launch_spectral_fp64(const OpacityLaunch& L, cudaStream_t stream, int num_sms);
+// Spectral opacities (phase kernels over chunks of points).  The scratch of
+// one call holds spectral_scratch_bytes(chunk, n_energies) bytes for chunks of
+// spectral_chunk_points(n_energies) points (about kSpecChunkRecords
+// (point, energy) records of 256 bytes).
+constexpr int64_t kSpecChunkRecords = 131072;
+int64_t spectral_chunk_points(int n_energies);
+size_t spectral_scratch_bytes(int64_t chunk_points, int n_energies);
+cudaError_t launch_spectral(const OpacityLaunch& L, cudaStream_t stream, int num_sms,
+                            void* scratch, int64_t chunk_points);
+cudaError_t spectral_mixed_counts(unsigned long long* counts, bool reset);
 struct DistrLaunch
 {
     int64_t npts;

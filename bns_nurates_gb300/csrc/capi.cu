@@ -187,6 +187,7 @@ int fill_common(const MyQuadrature* q1, const MyQuadrature* q2, const OpacityFla
         L->lx2[i] = log(x);
         L->l1m[i] = log1p(-x);
         L->l1p[i] = log1p(x);
+        L->lx1[i] = log(L->x1[i]);
     }
     // unordered energy pairs (a <= b), ordered by the sum of the energy
     // factors so that neighbouring lanes see similar Fermi-integral arguments
@@ -364,6 +365,22 @@ int bnsn_phase_times(double* ms, int64_t* launches)
 
 int64_t bnsn_kernel_launches(void) { return g_launches.load(); }
 
+int bnsn_spectral_mixed_stats(int64_t* counts, int reset)
+{
+    g_err.clear();
+    if (!counts)
+        return fail(BNSN_ERR_ARG, "NULL output");
+    unsigned long long c[4] = {0ull, 0ull, 0ull, 0ull};
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess)
+        e = spectral_mixed_counts(c, reset != 0);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "reading the spectral statistics");
+    for (int k = 0; k < 4; ++k)
+        counts[k] = (int64_t)c[k];
+    return BNSN_OK;
+}
+
 
 int bnsn_version(void) { return 100; }
 
@@ -526,21 +543,32 @@ int bnsn_spectral_opacities(const MyQuadrature* quad_1d, const OpacityFlags* fla
                 return fail(BNSN_ERR_ARG, "an output pointer is NULL");
             L.sout[q * 4 + s] = o[q][s];
         }
+    L.mixed = precision == BNSN_MIXED;
     DeviceState* st;
     if ((rc = attach_device(&L, &st)))
         return rc;
     L.e_stride = n_energies;
-    for (int e0 = 0; e0 < n_energies; e0 += 64)
+    if (npts == 0 || n_energies == 0)
+        return BNSN_OK;
+    const int ne_max     = n_energies < 64 ? n_energies : 64;
+    const int64_t chunk  = std::min<int64_t>(npts, spectral_chunk_points(ne_max));
+    void* ws             = nullptr;
+    cudaError_t e = cudaMallocFromPoolAsync(&ws, spectral_scratch_bytes(chunk, ne_max), st->pool,
+                                            (cudaStream_t)stream);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "spectral scratch allocation");
+    for (int e0 = 0; e0 < n_energies && e == cudaSuccess; e0 += 64)
     {
         L.n_energies = (n_energies - e0) < 64 ? (n_energies - e0) : 64;
         L.e_offset   = e0;
-        for (int e = 0; e < L.n_energies; ++e)
-            L.energies[e] = energies[e0 + e];
-        cudaError_t e = launch_spectral_fp64(L, (cudaStream_t)stream, st->num_sms);
-        if (e != cudaSuccess)
-            return cuda_fail(e, "spectral kernel launch");
+        for (int k = 0; k < L.n_energies; ++k)
+            L.energies[k] = energies[e0 + k];
+        e = launch_spectral(L, (cudaStream_t)stream, st->num_sms, ws, chunk);
     }
-    return BNSN_OK;
+    const cudaError_t ef = cudaFreeAsync(ws, (cudaStream_t)stream);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "spectral kernel launch");
+    return ef == cudaSuccess ? BNSN_OK : cuda_fail(ef, "spectral scratch release");
 }
 
 int bnsn_distr_from_m1(const bnsn_m1_soa* m1, const bnsn_distr_soa* out, int64_t npts,

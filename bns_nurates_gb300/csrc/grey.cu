@@ -35,6 +35,7 @@
 
 #include "bnsn_df.cuh"
 #include "bnsn_fp32.cuh"
+#include "bnsn_mixed.cuh"
 #include "bnsn_fp64.cuh"
 #include "bnsn_internal.h"
 
@@ -580,23 +581,6 @@ struct Gp19Warp
     float pf[2][kGp19MaxW];
 };
 
-// Bracket of lw on a log-w axis of d3 entries (binary search, first interval).
-template <class R>
-__device__ __forceinline__ int bracket_sorted(R lw, const R* ax, int d3, R* t)
-{
-    int lo = 0, hi = d3 - 2;
-    while (lo < hi)
-    {
-        const int mid = (lo + hi) >> 1;
-        if (lw <= ax[mid + 1])
-            hi = mid;
-        else
-            lo = mid + 1;
-    }
-    *t = (lw - ax[lo]) / (ax[lo + 1] - ax[lo]);
-    return lo;
-}
-
 // IMPL: 0 HR98, 1 BRT06, 2 GP19.  ADD: accumulate onto the pair sums.
 template <bool MIXED, int IMPL>
 __global__ void __launch_bounds__(kWarps * 32)
@@ -915,92 +899,6 @@ __device__ __forceinline__ void neps_items_fp64(const NepsPoint& NP, const Distr
             acc[4 + s] += Wr * (AB1 + AB2);
             acc[8 + s] += Wr * (nu * EM1 + nub * EM2);
             acc[12 + s] += Wr * (nu * AB1 + nub * AB2);
-        }
-    }
-}
-
-// Per-point data of the mixed item loop.
-struct NepsMixed
-{
-    dfm::df reta[2][5]; // unreflected F_1..F_5 at eta for e- (0) and e+ (1)
-    dfm::df eta[2];
-    float wt[4], wf[4];
-    double invTt[4], etat[4], lbf[4], invTf[4], cf[4]; // exponent arguments in FP64
-};
-
-// TotalNuF (distribution.hpp:298-315) and 1 - TotalNuF in FP32 with the
-// exponent arguments formed in FP64 (they cancel: omega/T_t - eta_t, and
-// log beta_f + c_f log omega - omega/T_f); lw = log omega.  The blocking
-// factor is formed from the complements of the two parts (w_t + w_f = 1 for
-// the reconstructed distribution), so it keeps its relative precision where
-// the occupation approaches 1.
-__device__ __forceinline__ void total_nu_f32(double omega, double lw, const NepsMixed& Q, float* g,
-                                             float* gm)
-{
-#pragma unroll
-    for (int s = 0; s < 4; ++s)
-    {
-        const float arg = (float)fma(omega, Q.invTt[s], -Q.etat[s]);
-        const float t   = expf(-fabsf(arg));
-        const float inv = 1.f / (t + 1.f);
-        const float ft  = arg > 0.f ? t * inv : inv;
-        const float ftm = arg > 0.f ? inv : t * inv;
-        const float fn  = expf((float)fma(Q.cf[s], lw, fma(-omega, Q.invTf[s], Q.lbf[s])));
-        g[s]            = Q.wt[s] * ft + Q.wf[s] * fn;
-        gm[s]           = Q.wt[s] * ftm + Q.wf[s] * (1.f - fn);
-    }
-}
-
-// NEPSExpFunc (functions.hpp:4401-4413) in FP32 for the FP64 argument d;
-// e^{-|d|} takes the FP32 exponential of the rounded argument times the
-// first-order correction for its remainder, expm1 keeps 1 - e^{-|d|}
-// accurate for small |d|.
-__device__ __forceinline__ float neps_exp_f32(double d, bool neg)
-{
-    const double ad = fabs(d);
-    const float a   = (float)ad;
-    const float alo = (float)(ad - (double)a); // e^{-alo} = 1 - alo to FP32 precision
-    const float ea  = expf(-a);
-    const float e   = ea * (1.f - alo);
-    const float dn  = -expm1f(-a) + ea * alo + (d == 0. ? 1.f : 0.f);
-    return (neg ? 1.f : -e) / dn;
-}
-
-// Taylor branches of neps_pair (kernel_nes.hpp:82-132) for w or w' near 0,
-// in FP64: dimensionless r1 = R(w, w'), r2 = R(w', w) of lepton e.  Rare in the
-// item loop, so kept out of line to keep the loop's code small.
-__device__ __noinline__ void neps_taylor(const NepsPoint& P, int e, double w, double wp,
-                                         double x, double y, int sign1, int sign2, double* r1,
-                                         double* r2)
-{
-    const double eta  = e ? P.eta1 : P.eta0;
-    const double* f0e = e ? P.fe1 : P.fe0;
-    const double fd0  = e ? P.fd01 : P.fd00;
-    if (x > eta * 1e-3)
-    {
-        double fx[3];
-        fdi_orders<0, 2>(eta - x, fx);
-        const double f[5] = {fx[2] - f0e[2], fx[1], f0e[1],
-                             fx[0] + y * fermi_distr(0., 1., eta - x) / 6., f0e[0] - y * fd0 / 6.};
-#pragma unroll
-        for (int s = 0; s < 4; ++s)
-        {
-            double b1, b2;
-            neps_couplings(e, s, &b1, &b2);
-            r1[s] = mb_int_one(x, y, sign1, b1, b2, f);
-            r2[s] = mb_int_one(x, y, sign2, b1, b2, f);
-        }
-    }
-    else
-    {
-        const double f[3] = {fd0, f0e[0], f0e[1]};
-#pragma unroll
-        for (int s = 0; s < 4; ++s)
-        {
-            double b1, b2;
-            neps_couplings(e, s, &b1, &b2);
-            r1[s] = mb_int_two(w, wp, x, y, b1, b2, f);
-            r2[s] = mb_int_two(wp, w, x, y, b1, b2, f);
         }
     }
 }

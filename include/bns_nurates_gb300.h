@@ -460,6 +460,14 @@ int bnsn_phase_timing(int enable);
 int bnsn_phase_times(double* ms, int64_t* launches);
 /* Number of kernels this library has launched in the process. */
 int64_t bnsn_kernel_launches(void);
+/* Mixed-precision spectral path on the current device since the last reset:
+ * counts[0] (point, energy) pairs evaluated, counts[1] pairs recomputed in FP64
+ * in some part because the FP32 error guards failed (terms that cancel) or a
+ * part could not run in FP32, counts[2] pair + brem recomputations, counts[3]
+ * NES recomputations.  reset != 0 zeroes the counters after reading;
+ * synchronises the device.  A diagnostic with no counterpart in the
+ * reference. */
+int bnsn_spectral_mixed_stats(int64_t* counts, int reset);
 
 const char* bnsn_status_string(int status);
 /* Text of the most recent error on the calling thread ("" if none). */

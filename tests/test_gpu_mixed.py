@@ -120,3 +120,68 @@ def test_mixed_close_to_fp64_gpu_and_deterministic(cuda):
     r = rel_err(a, c, floor=1e-300)
     assert np.percentile(r, 99.9) < MIXED_TOL
     assert np.isfinite(a).all() == np.isfinite(c).all()
+
+
+def _spec_oracle_with_sens(port, port_fma, eos, m1, flags, pars, nq, energies, stim=1,
+                           distr=None):
+    q = port.gauss_legendre(nq)
+    kw = dict(distr=distr, stimulated=stim, nthreads=NTHREADS)
+    want = port.spectral(eos, m1, flags, pars, q, energies, **kw)
+    sens = rel_err(port_fma.spectral(eos, m1, flags, pars, q, energies, **kw), want,
+                   floor=1e-300)
+    for row in (1, 7):
+        e2 = np.array(eos, copy=True)
+        e2[row] *= 1. + 2. ** -51
+        sens = np.maximum(sens, rel_err(port.spectral(e2, m1, flags, pars, q, energies, **kw),
+                                        want, floor=1e-300))
+    return want, sens
+
+
+SPEC_CASES = [
+    # (name, flags, pars, nq, stim, n_energies)
+    ("spectral all reactions, GP19, n=20", (1, 1, 1, 1, 1), (1, 0, 1, 1, 1, 2, 1, 0), 20, 1, 24),
+    ("spectral all reactions, HR98, n=10", (1, 1, 1, 1, 1), (1, 0, 1, 1, 1, 0, 1, 0), 10, 1, 24),
+    ("spectral NES only, n=12, not stimulated", (0, 0, 0, 1, 0), (1, 0, 1, 1, 1, 0, 1, 0), 12,
+     0, 40),
+    ("spectral pair+BRT06, n=8, neglect blocking", (0, 1, 1, 0, 0), (0, 1, 0, 0, 0, 1, 0, 1), 8,
+     1, 24),
+    ("spectral GP19 brem only, n=12, no medium", (0, 0, 1, 0, 0), (1, 0, 1, 1, 1, 2, 0, 0), 12,
+     1, 24),
+]
+
+
+@pytest.mark.parametrize("name,flags,pars,nq,stim,ne", SPEC_CASES, ids=[c[0] for c in SPEC_CASES])
+def test_mixed_spectral_vs_oracle(cuda, port, port_fma, name, flags, pars, nq, stim, ne):
+    eos, m1 = bn.synthetic_points(424242, 192, first=55)
+    energies = np.logspace(np.log10(0.5), np.log10(300.), ne)
+    e = cuda.from_numpy(eos).cuda()
+    m = cuda.from_numpy(m1).cuda()
+    got = bn.spectral_opacities(e, m, bn.opacity_flags(*flags), _params(pars),
+                                bn.gauss_legendre(nq), energies, stimulated=stim,
+                                precision="mixed")
+    cuda.cuda.synchronize()
+    want, sens = _spec_oracle_with_sens(port, port_fma, eos, m1, flags, pars, nq, energies,
+                                        stim=stim)
+    _check(got.cpu().numpy(), want, sens, name)
+
+
+def test_mixed_spectral_close_to_fp64_gpu(cuda):
+    """Bulk statistics (no oracle): p99.9 of the spectral mixed-vs-FP64
+    deviation below 1e-6 over 4096 points x 24 energies; repeat calls are
+    bitwise identical."""
+    eos, m1 = bn.synthetic_points(8, 4096, first=3 * 10 ** 6)
+    energies = np.logspace(0., np.log10(300.), 24)
+    e = cuda.from_numpy(eos).cuda()
+    m = cuda.from_numpy(m1).cuda()
+    fl, pr, q = bn.opacity_flags(), _params((1, 0, 1, 1, 1, 2, 1, 0)), bn.gauss_legendre(20)
+    bn.spectral_mixed_stats(reset=True)
+    a = bn.spectral_opacities(e, m, fl, pr, q, energies, precision="mixed").cpu().numpy()
+    st = bn.spectral_mixed_stats(reset=True)
+    assert st["evaluated"] == 4096 * 24
+    assert 0 <= st["fp64"] <= st["evaluated"] and st["fp64"] <= st["pb_fp64"] + st["nes_fp64"]
+    b = bn.spectral_opacities(e, m, fl, pr, q, energies, precision="mixed").cpu().numpy()
+    c = bn.spectral_opacities(e, m, fl, pr, q, energies, precision="fp64").cpu().numpy()
+    assert np.array_equal(a, b)
+    r = rel_err(a, c, floor=1e-300)
+    assert np.percentile(r, 99.9) < MIXED_TOL
+    assert (np.isfinite(a) == np.isfinite(c)).all()
