@@ -124,11 +124,12 @@ namespace {
 // NEPS prefactor, NEPSExpFunc and the occupations).  rw[e] are the
 // unreflected F_1..F_5 at aw[e] = eta_e - nu/T, staged per energy.  DF: R in
 // df (the accurate pass), else rounded to FP32 per lepton.
+// W, WP are w, wp in df.
 template <bool DF>
 __device__ __forceinline__ void neps_r_core(const NepsPoint& P, const NepsMixed& Q,
                                             const dfm::FdiTab* ftab, double w, double wp,
-                                            const dfm::df (*rw)[5], const dfm::df* aw,
-                                            dfm::df* Rd, float* Rf)
+                                            dfm::df W, dfm::df WP, const dfm::df (*rw)[5],
+                                            const dfm::df* aw, dfm::df* Rd, float* Rf)
 {
     using namespace dfm;
     const double x = (w > wp) ? w : wp;
@@ -143,9 +144,12 @@ __device__ __forceinline__ void neps_r_core(const NepsPoint& P, const NepsMixed&
         else
             Rf[s] = 0.f;
     }
-    const df W = from_double(w), WP = from_double(wp);
     const df S = add(W, WP), Pp = mul(W, WP), Dn = mul(Pp, Pp);
-    const df X = from_double(x), Y = from_double(y);
+    const df X = n1 ? W : WP, Y = n1 ? WP : W;
+    // bracket arguments from FP64 differences (eta up to ~1e3 needs 53 bits)
+    const double dd = w - wp, ad = fabs(dd);
+    const df dlt    = from_double(dd);    // w - wp
+    const df adw    = n1 ? dlt : neg(dlt); // |w - wp|
     const int nlep = P.eta0 > 30. ? 1 : 2; // e+ terms below 1e-13 of e- for eta_e > 30
 #pragma unroll 1
     for (int e = 0; e < nlep; ++e)
@@ -154,15 +158,14 @@ __device__ __forceinline__ void neps_r_core(const NepsPoint& P, const NepsMixed&
         if (y > eta * 1e-3)
         {
             const df awp = from_double(eta - wp);
-            const double adw = fabs(w - wp);
-            const df aab = from_double(eta - adw);
+            const df aab = from_double(eta - ad);
             df rwp[5], rab[5];
             fdi_raw15(awp, rwp, 1, ftab);
             fdi_raw15(aab, rab, 3, ftab);
             rab[0] = rab[1] = Q.reta[e][0];
             df dw[5], d5[5];
-            fdi_diff15(rw[e], rwp, aw[e], awp, from_double(w - wp), dw);
-            fdi_diff15(rab, Q.reta[e], aab, Q.eta[e], from_double(adw), d5);
+            fdi_diff15(rw[e], rwp, aw[e], awp, dlt, dw);
+            fdi_diff15(rab, Q.reta[e], aab, Q.eta[e], adw, d5);
             const df dabs[3] = {d5[2], d5[3], d5[4]};
             const df T1 = add(dw[3], mul(add(mul(S, dw[2]), mul(mul(Pp, 3.f), dw[1])), 2.f));
             const df U  = add(mul(X, dabs[1]), mul(mul(mul(X, X), 2.f), dabs[0]));
@@ -203,9 +206,10 @@ __device__ __forceinline__ void neps_r_core(const NepsPoint& P, const NepsMixed&
 
 __device__ __forceinline__ void neps_r_mixed(const NepsPoint& P, const NepsMixed& Q,
                                              const dfm::FdiTab* ftab, double w, double wp,
-                                             const dfm::df (*rw)[5], const dfm::df* aw, float* R)
+                                             dfm::df W, dfm::df WP, const dfm::df (*rw)[5],
+                                             const dfm::df* aw, float* R)
 {
-    neps_r_core<false>(P, Q, ftab, w, wp, rw, aw, nullptr, R);
+    neps_r_core<false>(P, Q, ftab, w, wp, W, WP, rw, aw, nullptr, R);
 }
 
 } // namespace
@@ -271,7 +275,7 @@ __device__ __forceinline__ void nes_spec_masks(const Distr& d, NesSpec* Z)
 // for absorption ((1 - g) e^{-(w' - w)^+}); -inf when there are no nodes.
 // FP32 throughout: sigma is only a scale, its error cancels exactly.
 __device__ __forceinline__ void nes_spec_scan(const NesSpec& Z, float w, float nu, float lnu,
-                                              const double* x, const double* lx, int n, int a0,
+                                              const double* x, const dfm::df* lx, int n, int a0,
                                               int step, bool nbb, float* sig)
 {
     float se = -INFINITY, sa = -INFINITY;
@@ -279,7 +283,7 @@ __device__ __forceinline__ void nes_spec_scan(const NesSpec& Z, float w, float n
     {
         const bool first = a < n;
         const int i      = first ? a : a - n;
-        const float xi = (float)x[i], li = (float)lx[i];
+        const float xi = (float)x[i], li = lx[i].hi;
         const float wp  = first ? w * xi : w / xi;
         const float nub = first ? nu * xi : nu / xi;
         const float lnb = first ? lnu + li : lnu - li;
@@ -314,27 +318,26 @@ __device__ __forceinline__ float exp_of(dfm::df x) { return expf(x.hi) * (1.f + 
 // absorption factor for w' > w, and dn = 1 - E (NEPSExpFunc,
 // functions.hpp:4401-4413).  de[s], da[s] bound the dropped components of
 // te[s], ta[s].
+// Node arguments in df: W = nu/T, WP = nubar/T, NB = nubar, LB = log nubar
+// (w, wp the same in FP64 for the branch tests of the kernel).
 __device__ __forceinline__ void nes_spec_node(const NepsPoint& P, const NepsMixed& Q,
                                               const NesSpec& Z, const dfm::FdiTab* ftab,
-                                              double w, double wp, double nub, double lnb,
-                                              float wa, float sig_e, float sig_a, bool nbb,
-                                              const dfm::df (*rw)[5], const dfm::df* aw,
-                                              float* te, float* ta, float* de, float* da)
+                                              double w, double wp, dfm::df W, dfm::df WP,
+                                              dfm::df NB, dfm::df LB, float wa, float sig_e,
+                                              float sig_a, bool nbb, const dfm::df (*rw)[5],
+                                              const dfm::df* aw, float* te, float* ta, float* de,
+                                              float* da)
 {
     using namespace dfm;
     float R[4];
-    neps_r_mixed(P, Q, ftab, w, wp, rw, aw, R);
+    neps_r_mixed(P, Q, ftab, w, wp, W, WP, rw, aw, R);
     const bool first = wp < w;
-    const double Dd  = fabs(w - wp);
-    const float a    = (float)Dd;
-    const float alo  = (float)(Dd - (double)a);
-    const float ea   = expf(-a);
-    const float dn   = -expm1f(-a) + ea * alo; // 1 - e^{-D}
-    const df D  = from_double(Dd);
+    const df D       = first ? sub(W, WP) : sub(WP, W); // |w - wp|
+    const float ea   = expf(-D.hi);
+    const float dn   = -expm1f(-D.hi) + ea * D.lo; // 1 - e^{-D}
     const df Se = first ? add(D, sig_e) : mk(sig_e);
     const df Sa = first ? mk(sig_a) : add(D, sig_a);
-    const df NB = from_double(nub), LB = from_double(lnb);
-    const float c = (first ? wa : -wa) * ((float)wp * (float)wp) / dn;
+    const float c = (first ? wa : -wa) * (WP.hi * WP.hi) / dn;
     float gnb = 0.f, unb = 0.f; // neglected blocking: (1 - g) -> 1
     if (nbb)
     {
@@ -402,20 +405,20 @@ __device__ __forceinline__ void nes_spec_node(const NepsPoint& P, const NepsMixe
 // scaled units, rounded to FP64.
 __device__ __forceinline__ void nes_spec_node_df(const NepsPoint& P, const NepsMixed& Q,
                                                  const NesSpec& Z, const dfm::FdiTab* ftab,
-                                                 double w, double wp, double nub, double lnb,
-                                                 double wa, float sig_e, float sig_a, bool nbb,
-                                                 const dfm::df (*rw)[5], const dfm::df* aw,
-                                                 double* te, double* ta, float* de, float* da)
+                                                 double w, double wp, dfm::df W, dfm::df WP,
+                                                 dfm::df NB, dfm::df LB, double wa, float sig_e,
+                                                 float sig_a, bool nbb, const dfm::df (*rw)[5],
+                                                 const dfm::df* aw, double* te, double* ta,
+                                                 float* de, float* da)
 {
     using namespace dfm;
     df R[4];
-    neps_r_core<true>(P, Q, ftab, w, wp, rw, aw, R, nullptr);
+    neps_r_core<true>(P, Q, ftab, w, wp, W, WP, rw, aw, R, nullptr);
     const bool first = wp < w;
-    const df D       = from_double(fabs(w - wp));
+    const df D       = first ? sub(W, WP) : sub(WP, W);
     const df dn      = add(neg(exp_df(neg(D))), 1.f); // 1 - e^{-D}, D > 0
     const df Se = first ? add(D, sig_e) : mk(sig_e);
     const df Sa = first ? mk(sig_a) : add(D, sig_a);
-    const df NB = from_double(nub), LB = from_double(lnb), WP = from_double(wp);
     const df c  = div(mul(from_double(first ? wa : -wa), mul(WP, WP)), dn);
     df gnb = mk(0.f);
     float unb = 0.f;

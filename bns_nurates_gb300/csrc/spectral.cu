@@ -199,7 +199,7 @@ struct PbWarp
     Hr98Point hr;
     double brt06_pre;
     int same_cf;
-    double nb[kMaxM];
+    double nb[kMaxM], zb[kMaxM]; // nubar and nubar / T
     double gb[kMaxM][4];
     double fmz[kMaxM][5], fpz[kMaxM][5];
     double fmy[kEChunk][5], fpy[kEChunk][5];
@@ -337,6 +337,7 @@ __global__ void __launch_bounds__(kWarps * 32)
             const int i     = a < n ? a : a - n;
             const double nu = a < n ? ts * S.x[i] : ts / S.x[i];
             W.nb[a]         = nu;
+            W.zb[a]         = nu / T;
             total_nu_f4(nu, W.d, same_cf, W.gb[a]);
             if (MIX)
             {
@@ -437,8 +438,14 @@ __global__ void __launch_bounds__(kWarps * 32)
                         double pe[4] = {0., 0., 0., 0.}, pa[4] = {0., 0., 0., 0.};
                         double be = 0., ba = 0.;
                         if (L.use_pair)
-                            pair_kernel(T, eta_e, nu, nub, w, nub / T, W.fmy[c], W.fpy[c],
-                                        W.fmz[a], W.fpz[a], W.fe3, W.fe4, pe, pa);
+                        {
+                            if (MIX) // one exponential, no division by T
+                                pair_kernel_one_exp(T, eta_e, w, W.zb[a], W.fmy[c], W.fpy[c],
+                                                    W.fmz[a], W.fpz[a], W.fe3, W.fe4, pe, pa);
+                            else
+                                pair_kernel(T, eta_e, nu, nub, w, W.zb[a], W.fmy[c], W.fpy[c],
+                                            W.fmz[a], W.fpz[a], W.fe3, W.fe4, pe, pa);
+                        }
                         if (L.use_brem && !b32)
                         {
                             if (L.brem_impl == 0)
@@ -578,20 +585,21 @@ struct NesWarpMixed
     NesSpec Z;
     dfm::df rw[kEChunk][2][5]; // unreflected F_1..F_5 at eta_e - nu/T per energy and lepton
     dfm::df aw[kEChunk][2];
-    double lnu[kEChunk];
+    dfm::df lnu[kEChunk];
 };
 
 template <int MODE>
 struct NesShared
 {
-    double x[kMaxQ], lx[kMaxQ], B1[kMaxM];
+    double x[kMaxQ], xinv[kMaxQ], B1[kMaxM];
+    dfm::df lxd[kMaxQ];
     dfm::FdiTab ftab;
     NesWarp w[kWarps];
     NesWarpMixed m[(MODE == kSpecMixed || MODE == kSpecAcc) ? kWarps : 1];
 };
 
 template <int MODE>
-__global__ void __launch_bounds__(kWarps * 32)
+__global__ void __launch_bounds__(kWarps * 32, MODE == kSpecMixed ? 4 : 1)
     spec_nes_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
                     const double* __restrict__ dsc, EnergyRec* __restrict__ rec,
                     const uint64_t* __restrict__ flags, int G)
@@ -602,8 +610,9 @@ __global__ void __launch_bounds__(kWarps * 32)
     NesShared<MODE>& S = *reinterpret_cast<NesShared<MODE>*>(s_raw);
     for (int k = threadIdx.x; k < kMaxQ; k += blockDim.x)
     {
-        S.x[k]  = L.x1[k];
-        S.lx[k] = L.lx1[k];
+        S.x[k]    = L.x1[k];
+        S.xinv[k] = 1. / L.x1[k];
+        S.lxd[k]  = dfm::from_double(L.lx1[k]);
     }
     for (int k = threadIdx.x; k < kMaxM; k += blockDim.x)
         S.B1[k] = L.B1[k];
@@ -629,7 +638,7 @@ __global__ void __launch_bounds__(kWarps * 32)
         const int per_round = 32 / Gq;
         const int64_t p     = p0 + q;
         const double T = L.eos[1][p], mu_e = L.eos[7][p];
-        const double eta_e = mu_e / T;
+        const double eta_e = mu_e / T, invT = 1. / T;
         EnergyRec* R       = rec + q * ne;
         __syncwarp();
         load_distr(dsc, q, &W.d, lane);
@@ -695,7 +704,7 @@ __global__ void __launch_bounds__(kWarps * 32)
                 }
                 else if (m32 && y >= kSpecNesMinW)
                 {
-                    X.lnu[c] = log(nu);
+                    X.lnu[c] = dfm::from_double(log(nu));
 #pragma unroll 1
                     for (int e = 0; e < 2; ++e)
                     {
@@ -727,7 +736,7 @@ __global__ void __launch_bounds__(kWarps * 32)
                 if (MIX)
                 {
                     // scale of this energy: group-wide maximum of the lanes' scans
-                    nes_spec_scan(X.Z, (float)w, (float)nu, (float)X.lnu[run ? c : 0], S.x, S.lx,
+                    nes_spec_scan(X.Z, (float)w, (float)nu, X.lnu[run ? c : 0].hi, S.x, S.lxd,
                                   n, run ? grp : M, Gq, nbb, sig);
                     for (int o = 1; o < Gq; o <<= 1)
                     {
@@ -739,19 +748,25 @@ __global__ void __launch_bounds__(kWarps * 32)
                     sne    = sn * exp((double)sig[0]);
                     sna    = sn * exp((double)sig[1]);
                 }
+                const dfm::df Wd = dfm::from_double(w);
                 if (run)
                 {
                     for (int a = grp; a < M; a += Gq)
                     {
                         const int i      = a < n ? a : a - n;
                         const double wa  = S.B1[a];
-                        const double nub = a < n ? nu * S.x[i] : nu / S.x[i];
+                        const double nub =
+                            a < n ? nu * S.x[i] : (MIX ? nu * S.xinv[i] : nu / S.x[i]);
+                        // mixed passes: nubar/T and log nubar without divisions
+                        const double wp  = MIX ? nub * invT : nub / T;
+                        const dfm::df NB = dfm::from_double(nub), WPd = dfm::from_double(wp);
+                        const dfm::df LB =
+                            dfm::add(X.lnu[c], a < n ? S.lxd[i] : dfm::neg(S.lxd[i]));
                         if (ACC)
                         {
-                            const double lnb = X.lnu[c] + (a < n ? S.lx[i] : -S.lx[i]);
                             double te[4], ta[4];
                             float de[4], da[4];
-                            nes_spec_node_df(NP, X.Q, X.Z, &S.ftab, w, nub / T, nub, lnb, wa,
+                            nes_spec_node_df(NP, X.Q, X.Z, &S.ftab, w, wp, Wd, WPd, NB, LB, wa,
                                              sig[0], sig[1], nbb, X.rw[c], X.aw[c], te, ta, de,
                                              da);
 #pragma unroll
@@ -766,9 +781,8 @@ __global__ void __launch_bounds__(kWarps * 32)
                         }
                         else if (MIX)
                         {
-                            const double lnb = X.lnu[c] + (a < n ? S.lx[i] : -S.lx[i]);
                             float te[4], ta[4], de[4], da[4];
-                            nes_spec_node(NP, X.Q, X.Z, &S.ftab, w, nub / T, nub, lnb, (float)wa,
+                            nes_spec_node(NP, X.Q, X.Z, &S.ftab, w, wp, Wd, WPd, NB, LB, (float)wa,
                                           sig[0], sig[1], nbb, X.rw[c], X.aw[c], te, ta, de, da);
 #pragma unroll
                             for (int s = 0; s < 4; ++s)
