@@ -11,8 +11,9 @@ from ._capi import (BREM_BRT06, BREM_GP19, BREM_HR98, FP64, MIXED,  # noqa: F401
 from .api import (BlocksPlan, BnsnError, ComputeM1Opacities, ComputeM1OpacitiesNotStimulated,  # noqa: F401
                   ComputeSpectralOpacitiesNotStimulatedAbs,
                   ComputeSpectralOpacitiesStimulatedAbs, distr_from_m1, flags_tuple,
-                  fp32_peak_tflops, fp64_peak_tflops, gauss_legendre, kernel_launches, m1_opacities,
-                  m1_opacities_host, nu_equilibrium, opacity_flags, opacity_params, params_tuple,
+                  fp32_peak_tflops, fp64_peak_tflops, gauss_legendre, gp19_table_from_header,
+                  kernel_launches, load_gp19_header, m1_opacities,
+                  m1_opacities_host, nonfinite_outputs, nu_equilibrium, opacity_flags, opacity_params, params_tuple,
                   phase_times, phase_timing, quad_arrays, set_gp19_table, spectral_mixed_stats,
                   spectral_opacities, synthetic_points)
 

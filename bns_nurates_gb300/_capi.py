@@ -158,6 +158,8 @@ SIGNATURES = {
     "bnsn_phase_times": (c_int, [P, P]),
     "bnsn_kernel_launches": (ctypes.c_int64, []),
     "bnsn_spectral_mixed_stats": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64), ctypes.c_int]),
+    "bnsn_gp19_load_header": (ctypes.c_int, [ctypes.c_char_p]),
+    "bnsn_nonfinite_outputs": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64), ctypes.c_int]),
     "bnsn_status_string": (ctypes.c_char_p, [c_int]),
     "bnsn_last_error": (ctypes.c_char_p, []),
     "bnsn_version": (c_int, []),

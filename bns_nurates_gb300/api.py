@@ -16,6 +16,7 @@ the module raises if that library is missing.
 """
 
 import ctypes
+import os
 
 import numpy as np
 
@@ -213,6 +214,57 @@ def set_gp19_table(tab):
     _check(C.load().bnsn_gp19_set_table(dims, *ptrs))
 
 
+def load_gp19_header(path):
+    """Load a GP19 table from a header in the reference's GP19Table.hpp format."""
+    _check(C.load().bnsn_gp19_load_header(os.fsencode(path)))
+
+
+_GP19_DIMS = ("GP19_nb_dims", "GP19_Ye_dims", "GP19_T_dims", "GP19_w_dims")
+_GP19_ARRAYS = (("nb", "GP19_nb_axis"), ("ye", "GP19_Ye_axis"), ("t", "GP19_T_axis"),
+                ("w", "GP19_w_axis"), ("lognb", "GP19_lognb_axis"),
+                ("logw", "GP19_logw_axis"), ("data", "GP19_data"))
+
+
+def gp19_table_from_header(path):
+    """Parse a header in the reference's GP19Table.hpp format into the table
+    dict of set_table (host only; the same declarations bnsn_gp19_load_header
+    reads)."""
+    import re
+    text = open(path).read()
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", " ", text)
+
+    def decl(name):
+        m = re.search(r"(?<![A-Za-z0-9_])" + name + r"(?![A-Za-z0-9_])\s*(\[[^\]]*\])?\s*=(?!=)",
+                      text)
+        return None if m is None else m.end()
+
+    dims = []
+    for name in _GP19_DIMS:
+        q = decl(name)
+        if q is None:
+            raise ValueError(f"{name} not declared in {path}")
+        dims.append(int(re.match(r"\s*(\d+)", text[q:]).group(1)))
+    tab = {"dims": tuple(dims)}
+    num = r"[-+]?(?:\d+\.?\d*|\.\d+)(?:[eE][-+]?\d+)?"
+    for key, name in _GP19_ARRAYS:
+        q = decl(name)
+        if q is None:
+            tab[key] = None
+            continue
+        depth, i = 0, text.index("{", q)
+        for j in range(i, len(text)):
+            depth += {"{": 1, "}": -1}.get(text[j], 0)
+            if depth == 0:
+                break
+        tab[key] = np.array([float(v) for v in re.findall(num, text[i:j + 1])])
+    for key, n in (("nb", dims[0]), ("ye", dims[1]), ("t", dims[2]), ("w", dims[3]),
+                   ("data", dims[0] * dims[1] * dims[2] * dims[3])):
+        if tab[key] is None or tab[key].size != n:
+            raise ValueError(f"GP19 {key} array missing or of the wrong length in {path}")
+    return tab
+
+
 def synthetic_points(seed, n, first=0, nthreads=0):
     """Seeded synthetic points on the host: (eos [11, n], m1 [12, n]) numpy."""
     import os
@@ -261,6 +313,14 @@ def spectral_mixed_stats(reset=False):
     c = (ctypes.c_int64 * 4)()
     _check(C.load().bnsn_spectral_mixed_stats(c, int(reset)))
     return dict(zip(("evaluated", "fp64", "pb_fp64", "nes_fp64"), (int(v) for v in c)))
+
+
+def nonfinite_outputs(reset=False):
+    """Outputs with a NaN or Inf on the current device since the last reset:
+    {"grey_points", "spectral_pairs"}."""
+    c = (ctypes.c_int64 * 2)()
+    _check(C.load().bnsn_nonfinite_outputs(c, int(reset)))
+    return {"grey_points": int(c[0]), "spectral_pairs": int(c[1])}
 
 
 def m1_opacities_host(eos, m1, flags, params, quad_1d, quad_2d=None, stim_abs=1,

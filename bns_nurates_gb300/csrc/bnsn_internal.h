@@ -106,6 +106,10 @@ size_t spectral_scratch_bytes(int64_t chunk_points, int n_energies);
 cudaError_t launch_spectral(const OpacityLaunch& L, cudaStream_t stream, int num_sms,
                             void* scratch, int64_t chunk_points);
 cudaError_t spectral_mixed_counts(unsigned long long* counts, bool reset);
+// Outputs holding a NaN or Inf since the last reset: grey points, spectral
+// (point, energy) pairs (synchronous reads of the current device's counters).
+cudaError_t grey_nonfinite_count(unsigned long long* count, bool reset);
+cudaError_t spectral_nonfinite_count(unsigned long long* count, bool reset);
 struct DistrLaunch
 {
     int64_t npts;

@@ -382,6 +382,24 @@ int bnsn_spectral_mixed_stats(int64_t* counts, int reset)
 }
 
 
+int bnsn_nonfinite_outputs(int64_t* counts, int reset)
+{
+    g_err.clear();
+    if (!counts)
+        return fail(BNSN_ERR_ARG, "NULL output");
+    unsigned long long g = 0ull, sp = 0ull;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess)
+        e = grey_nonfinite_count(&g, reset != 0);
+    if (e == cudaSuccess)
+        e = spectral_nonfinite_count(&sp, reset != 0);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "reading the non-finite output counters");
+    counts[0] = (int64_t)g;
+    counts[1] = (int64_t)sp;
+    return BNSN_OK;
+}
+
 int bnsn_version(void) { return 100; }
 
 const char* bnsn_last_error(void) { return g_err.c_str(); }

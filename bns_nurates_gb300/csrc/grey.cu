@@ -1402,6 +1402,11 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
 // ---------------------------------------------------------------------------
 // assembly (m1_opacities.hpp:1172-1294), one thread per point
 // ---------------------------------------------------------------------------
+
+// Points whose outputs hold a NaN or Inf (the reference propagates them from
+// bad inputs, e.g. GP19 outside its table); read by grey_nonfinite_count.
+__device__ unsigned long long g_grey_nonfinite;
+
 __global__ void __launch_bounds__(128)
     grey_final_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
                       const double* __restrict__ scratch)
@@ -1409,6 +1414,7 @@ __global__ void __launch_bounds__(128)
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < np;
          q += (int64_t)gridDim.x * blockDim.x)
     {
+        bool nonfinite      = false;
         const int64_t p     = L.pidx ? L.pidx[p0 + q] : p0 + q;
         const PointTab* P   = (const PointTab*)(scratch + q * kTabWords);
         const double T      = L.eos[1][p];
@@ -1471,8 +1477,13 @@ __global__ void __launch_bounds__(128)
             o[4] = (J > k::ThresholdJ) ? F / (c * J) * iso : 0.;
 #pragma unroll
             for (int qq = 0; qq < 5; ++qq)
+            {
                 L.out[qq * 4 + s][p] = o[qq];
+                nonfinite = nonfinite || !isfinite(o[qq]);
+            }
         }
+        if (nonfinite)
+            atomicAdd(&g_grey_nonfinite, 1ull);
     }
 }
 
@@ -1516,6 +1527,17 @@ cudaError_t launch_brem(const OpacityLaunch& L, int64_t p0, int64_t np, double* 
 }
 
 } // namespace
+
+cudaError_t grey_nonfinite_count(unsigned long long* count, bool reset)
+{
+    cudaError_t e = cudaMemcpyFromSymbol(count, g_grey_nonfinite, sizeof(*count));
+    if (e == cudaSuccess && reset)
+    {
+        const unsigned long long zero = 0ull;
+        e = cudaMemcpyToSymbol(g_grey_nonfinite, &zero, sizeof(zero));
+    }
+    return e;
+}
 
 cudaError_t launch_grey(const OpacityLaunch& L, cudaStream_t st, int sms, double* ws,
                         int64_t ws_points)

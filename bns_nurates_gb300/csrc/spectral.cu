@@ -86,6 +86,9 @@ enum SpecMode
 // recomputations.
 __device__ unsigned long long g_spec_counts[4];
 
+// (point, energy) pairs whose outputs hold a NaN or Inf.
+__device__ unsigned long long g_spec_nonfinite;
+
 // Lane group size for ne energy tasks of M nodes each (power of two <= 32)
 // minimising rounds x nodes per task.
 __host__ __device__ inline int pick_groups(int ne, int M)
@@ -939,6 +942,7 @@ __global__ void __launch_bounds__(kWarps * 32)
                 }
                 if (!fpb && !fnes)
                 {
+                    bool nonfinite = false;
                     double ge[4];
                     total_nu_f4(nu, D, same_cf, ge);
                     const double iso =
@@ -961,7 +965,11 @@ __global__ void __launch_bounds__(kWarps * 32)
                         L.sout[4 + s][o]  = ka;
                         L.sout[8 + s][o]  = js;
                         L.sout[12 + s][o] = ks;
+                        nonfinite = nonfinite || !isfinite(j) || !isfinite(ka) ||
+                                    !isfinite(js) || !isfinite(ks);
                     }
+                    if (nonfinite)
+                        atomicAdd(&g_spec_nonfinite, 1ull);
                 }
             }
             if (GUARD)
@@ -1080,6 +1088,17 @@ cudaError_t spectral_mixed_counts(unsigned long long* counts, bool reset)
     {
         const unsigned long long zero[4] = {0ull, 0ull, 0ull, 0ull};
         e = cudaMemcpyToSymbol(g_spec_counts, zero, sizeof(zero));
+    }
+    return e;
+}
+
+cudaError_t spectral_nonfinite_count(unsigned long long* count, bool reset)
+{
+    cudaError_t e = cudaMemcpyFromSymbol(count, g_spec_nonfinite, sizeof(*count));
+    if (e == cudaSuccess && reset)
+    {
+        const unsigned long long zero = 0ull;
+        e = cudaMemcpyToSymbol(g_spec_nonfinite, &zero, sizeof(zero));
     }
     return e;
 }

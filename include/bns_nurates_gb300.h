@@ -390,6 +390,13 @@ int bnsn_gp19_set_table(const int dims[4], const double* nb_axis,
                         const double* w_axis, const double* lognb_axis,
                         const double* logw_axis, const double* data);
 
+/* The same from a table header in the reference's format (the GP19Table.hpp
+ * that kernel_brem_GP19.hpp includes: GP19_{nb,Ye,T,w}_dims constants and the
+ * GP19_{nb,lognb,Ye,T,w,logw}_axis / GP19_data brace initialisers), read as
+ * text at run time; the log axes are optional.  BNSN_ERR_ARG when the file is
+ * missing or a declaration is absent or has the wrong length. */
+int bnsn_gp19_load_header(const char* path);
+
 /* ======================================================================
  * Part 3: per-point drop-ins, host-buffer batches, utilities
  * ====================================================================== */
@@ -468,6 +475,14 @@ int64_t bnsn_kernel_launches(void);
  * synchronises the device.  A diagnostic with no counterpart in the
  * reference. */
 int bnsn_spectral_mixed_stats(int64_t* counts, int reset);
+/* Outputs holding a NaN or Inf on the current device since the last reset:
+ * counts[0] grey points (any of the 20 outputs), counts[1] spectral (point,
+ * energy) pairs (any of the 16 outputs).  The kernels never trap: non-finite
+ * inputs, or GP19 brem outside its table, propagate into the outputs as in
+ * the reference, and these counters let a caller detect it without scanning
+ * the outputs.  reset != 0 zeroes the counters after reading; synchronises
+ * the device. */
+int bnsn_nonfinite_outputs(int64_t* counts, int reset);
 
 const char* bnsn_status_string(int status);
 /* Text of the most recent error on the calling thread ("" if none). */
