@@ -83,6 +83,12 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison")
+    ap.add_argument("--no-spectral", action="store_true",
+                    help="skip the spectral leg of the c2/c5 workloads")
+    ap.add_argument("--spectral-npts", type=int, default=262144,
+                    help="points of the spectral leg (24 energies each)")
+    ap.add_argument("--cond-npts", type=int, default=262144,
+                    help="points of the grey conditioning probe")
     return ap.parse_args()
 
 
@@ -447,6 +453,79 @@ def run_blocks(args, rank, world, local):
         torch.distributed.destroy_process_group()
 
 
+SPEC_ENERGIES = np.logspace(0., np.log10(300.), 24)
+
+
+def spectral_leg(args, bn, torch, eos, m1, flags, params, q, stream, world, dev):
+    """Spectral opacities (16 outputs x 24 energies per point) of the first
+    --spectral-npts points: device-timed points/s of --precision and, for the
+    mixed path, of the plain FP64 path on the same points, the mixed-vs-FP64
+    error and the mixed path's FP64-recomputation statistics."""
+    ns = min(eos.shape[1], args.spectral_npts)
+    eo, mo = eos[:, :ns].contiguous(), m1[:, :ns].contiguous()
+    precs = [args.precision] + (["fp64"] if args.precision == "mixed" else [])
+    outs, legs = {}, {}
+    for prec in precs:
+        o = torch.empty((16, ns, SPEC_ENERGIES.size), dtype=torch.float64, device=dev)
+
+        def sstep(prec=prec, o=o):
+            bn.spectral_opacities(eo, mo, flags, params, q, SPEC_ENERGIES, precision=prec,
+                                  out=o, stream=stream)
+
+        sstep()
+        if prec == "mixed":
+            bn.spectral_mixed_stats(reset=True)
+        ms = timed_steps(sstep, 1, stream, torch)
+        legs[prec] = {"value": world * ns / (ms * 1e-3), "unit": "points/s", "ms": ms,
+                      "steps": 1, "warmup": 1}
+        if prec == "mixed":
+            st = bn.spectral_mixed_stats(reset=True)
+            legs[prec]["fp64_recomputed"] = {k: v / max(1, st["evaluated"])
+                                             for k, v in st.items() if k != "evaluated"}
+        outs[prec] = o
+    res = {"points": ns, "energies": int(SPEC_ENERGIES.size),
+           "energy_range_mev": [1.0, 300.0], "outputs_per_energy": 16, **legs}
+    if "fp64" in outs and args.precision == "mixed":
+        a, b = outs["mixed"].cpu().numpy(), outs["fp64"].cpu().numpy()
+        r = rel_err(a, b)
+        res["mixed_over_fp64"] = legs["fp64"]["ms"] / legs["mixed"]["ms"]
+        res["accuracy"] = {"vs": "plain FP64 GPU path, every output, point and energy",
+                           "max_rel": float(r.max()), "p99_rel": float(np.percentile(r, 99)),
+                           "p999_rel": float(np.percentile(r, 99.9)),
+                           "frac_above_1e-6": float(np.mean(r > 1e-6))}
+
+        def spec64(e, o):
+            bn.spectral_opacities(e, mo, flags, params, q, SPEC_ENERGIES, precision="fp64",
+                                  out=o, stream=stream)
+
+        res["accuracy"].update(conditioned_error(torch, eo, spec64, tuple(outs["fp64"].shape),
+                                                 r, b))
+    return res
+
+
+def conditioned_error(torch, eos, run64, shape, r, ref):
+    """Splits the mixed-vs-FP64 error by the conditioning of each output: an
+    output is well conditioned when the FP64 path moves by at most 1e-9
+    (relative) under a two-ulp change of T or of mu_e; there the contract is
+    1e-6, elsewhere the reference's own result is not reproducible to that
+    level."""
+    sens = np.zeros(shape)
+    for row in (1, 7):
+        e2 = eos.clone()
+        e2[row] *= 1. + 2. ** -51
+        o = torch.empty(shape, dtype=torch.float64, device=eos.device)
+        run64(e2, o)
+        torch.cuda.synchronize()
+        sens = np.maximum(sens, rel_err(o.cpu().numpy(), ref))
+    well = sens <= 1e-9
+    return {"well_conditioned": {"criterion": "FP64 output moves <= 1e-9 under +2 ulp in T "
+                                              "or mu_e",
+                                 "points": int(shape[1]), "fraction": float(well.mean()),
+                                 "max_rel": float(np.max(np.where(well, r, 0.))),
+                                 "p999_rel": float(np.percentile(r[well], 99.9))
+                                 if well.any() else None}}
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
@@ -526,7 +605,8 @@ def main():
         ms64 = timed_steps(lambda: step("fp64", out64), k64, stream, torch) / k64
         fp64 = {"value": world * n / (ms64 * 1e-3), "unit": "points/s", "ms_per_step": ms64,
                 "steps": k64, "warmup": 1, "mixed_over_fp64": ms64 / ms_per_step}
-        r = rel_err(res, out64.cpu().numpy())
+        r64 = out64.cpu().numpy()
+        r = rel_err(res, r64)
         names = [f"{f}[{s}]" for f in ("eta_0", "kappa_0_a", "eta", "kappa_a", "kappa_s")
                  for s in ("nue", "anue", "nux", "anux")]
         accuracy = {"vs": "plain FP64 GPU path, every output of every point",
@@ -534,6 +614,16 @@ def main():
                     "p999_rel": float(np.percentile(r, 99.9)),
                     "frac_above_1e-6": float(np.mean(r > 1e-6)),
                     "max_rel_per_output": {nm: float(r[k].max()) for k, nm in enumerate(names)}}
+        # conditioning of each output: the FP64 path's own change when T or
+        # mu_e moves by two ulps, on the first points of the batch
+        nc = min(n, args.cond_npts)
+
+        def grey64(e, o):
+            bn.m1_opacities(e, m1[:, :nc].contiguous(), flags, params, q, out=o,
+                            precision="fp64", stream=stream)
+
+        accuracy.update(conditioned_error(torch, eos[:, :nc].contiguous(), grey64,
+                                          (20, nc), r[:, :nc], r64[:, :nc]))
 
     # end to end through the host-buffer C-ABI call, pinned host memory
     e2e = None
@@ -595,6 +685,12 @@ def main():
                                  "note": "algorithmic I/O bytes (23 inputs + 20 outputs "
                                          "x 8 B per point) over the step time"}
 
+    # spectral leg (c2, c5: grey plus spectral opacities at 24 log-spaced
+    # energies 1-300 MeV) on the first points of the step's batch
+    spectral = None
+    if args.workload in ("c2", "c5") and not args.no_spectral:
+        spectral = spectral_leg(args, bn, torch, eos, m1, flags, params, q, stream, world, dev)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         import oracle
@@ -623,7 +719,7 @@ def main():
                              % (23 * 8 * n / 1e6),
                        "parallelism": f"{world} independent point shards"},
             "fp64_gpu": fp64, "accuracy": accuracy,
-            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "spectral": spectral,
             "clocks": clk.summary(), "gpu_launches": launches,
             "phases_ms": {k: {"ms": v[0], "launches": v[1]} for k, v in phases.items() if v[1]},
             "generator_s": gen_s,
