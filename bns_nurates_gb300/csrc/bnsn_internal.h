@@ -73,6 +73,8 @@ void phase_mark(int phase, int end, cudaStream_t stream);
 
 // Grey opacities in chunks of ws_points points; ws holds ws_points per-point
 // scratch records of grey_point_scratch_bytes() (= kGreyRecordBytes) each.
+// With an auxiliary stream (launch_grey's aux, else nullptr) the chunks are
+// ws_points / 2 points, alternating between the two streams.
 constexpr size_t kGreyRecordBytes = 767 * sizeof(double);
 size_t grey_point_scratch_bytes();
 
@@ -95,7 +97,7 @@ int capi_device_info(DeviceInfo* info);                // current device (create
 constexpr int64_t kNoAllocPoints = 4096;
 cudaError_t noalloc_scratch(int device, double** ptr);
 cudaError_t launch_grey(const OpacityLaunch& L, cudaStream_t stream, int num_sms, double* ws,
-                        int64_t ws_points);
+                        int64_t ws_points, cudaStream_t aux = nullptr);
 // Spectral opacities (phase kernels over chunks of points).  The scratch of
 // one call holds spectral_scratch_bytes(chunk, n_energies) bytes for chunks of
 // spectral_chunk_points(n_energies) points (about kSpecChunkRecords

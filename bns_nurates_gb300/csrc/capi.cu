@@ -53,6 +53,7 @@ struct DeviceState
     void* stage  = nullptr; // staging area of the host-buffer APIs
     size_t stage_bytes = 0;
     cudaStream_t streams[2] = {nullptr, nullptr};
+    cudaStream_t aux   = nullptr; // second stream of the grey chunk pipeline
     cudaMemPool_t pool = nullptr; // grey scratch records
 };
 
@@ -99,6 +100,11 @@ int device_state(DeviceState** out)
         {
             st.num_sms = 0;
             return cuda_fail(e, "cudaMemPoolSetAttribute");
+        }
+        if ((e = cudaStreamCreateWithFlags(&st.aux, cudaStreamNonBlocking)) != cudaSuccess)
+        {
+            st.num_sms = 0;
+            return cuda_fail(e, "cudaStreamCreateWithFlags");
         }
     }
     *out = &st;
@@ -450,13 +456,16 @@ int bnsn_m1_opacities(const MyQuadrature* quad_1d, const MyQuadrature* quad_2d,
         return rc;
     if (npts == 0)
         return BNSN_OK;
-    const int64_t ws_points = std::min<int64_t>(npts, kGreyChunk);
+    // more than one chunk: two chunks in flight on the caller's stream and aux
+    const bool two          = npts > kGreyChunk;
+    const int64_t ws_points = two ? 2 * kGreyChunk : npts;
     double* ws = nullptr;
     cudaError_t e = cudaMallocFromPoolAsync((void**)&ws, ws_points * grey_point_scratch_bytes(),
                                            st->pool, (cudaStream_t)stream);
     if (e != cudaSuccess)
         return cuda_fail(e, "grey scratch allocation");
-    e = launch_grey(L, (cudaStream_t)stream, st->num_sms, ws, ws_points);
+    e = launch_grey(L, (cudaStream_t)stream, st->num_sms, ws, ws_points,
+                    two ? st->aux : nullptr);
     const cudaError_t ef = cudaFreeAsync(ws, (cudaStream_t)stream);
     if (e != cudaSuccess)
         return cuda_fail(e, "grey kernel launch");
