@@ -82,8 +82,10 @@ struct bnsn_blocks_plan
 {
     int device     = 0;
     int num_sms    = 0;
-    double* ws     = nullptr;
+    double* ws     = nullptr; // two halves of ws_pts records, one per stream
     int64_t ws_pts = 0;
+    cudaStream_t aux  = nullptr; // second stream of the chunk pipeline
+    cudaEvent_t ev[2] = {nullptr, nullptr};
     std::vector<Group> groups;
 };
 
@@ -179,9 +181,13 @@ int bnsn_blocks_plan_create(const bnsn_block* blocks, int nblocks, const Opacity
     for (const Group& G : P->groups)
         need = std::max(need, std::min<int64_t>(G.npts, tune ? kChunks[3] : G.chunk));
     P->ws_pts = std::max<int64_t>(need, 1);
-    cudaError_t e = cudaMalloc((void**)&P->ws, P->ws_pts * grey_point_scratch_bytes());
+    cudaError_t e = cudaMalloc((void**)&P->ws, 2 * P->ws_pts * grey_point_scratch_bytes());
     if (e != cudaSuccess)
         return cleanup(capi_cuda_fail(e, "plan scratch"));
+    if ((e = cudaStreamCreateWithFlags(&P->aux, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&P->ev[0], cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&P->ev[1], cudaEventDisableTiming)) != cudaSuccess)
+        return cleanup(capi_cuda_fail(e, "plan stream"));
     if (tune && total > 0)
     {
         cudaEvent_t e0, e1;
@@ -252,20 +258,38 @@ int bnsn_blocks_run(bnsn_blocks_plan_t plan, const bnsn_eos_soa* eos, const bnsn
     cudaGetDevice(&dev);
     if (dev != plan->device)
         return capi_fail(BNSN_ERR_ARG, "the plan was made on another device");
+    // all groups' chunks alternate between the caller's stream and the plan's
+    // second stream (the FP64 phases of one chunk beside the FP32 phases of
+    // the next), with one fork before the first and one join after the last
+    const cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e         = cudaEventRecord(plan->ev[0], st);
+    if (e == cudaSuccess)
+        e = cudaStreamWaitEvent(plan->aux, plan->ev[0], 0);
+    if (e != cudaSuccess)
+        return capi_cuda_fail(e, "blocks run");
+    int64_t k = 0;
+    int rc    = BNSN_OK;
     for (Group& G : plan->groups)
     {
         if (G.npts == 0)
             continue;
-        int rc = fill_points_soa(eos, m1, out, &G.L);
-        if (rc)
-            return rc;
+        if ((rc = fill_points_soa(eos, m1, out, &G.L)))
+            break;
         G.L.grid_scale = G.grid;
-        const cudaError_t e = launch_grey(G.L, (cudaStream_t)stream, plan->num_sms, plan->ws,
-                                          std::min<int64_t>(G.chunk, plan->ws_pts));
+        e = launch_grey_chunks(G.L, st, plan->aux, plan->num_sms, plan->ws,
+                               plan->ws + plan->ws_pts * (grey_point_scratch_bytes() / sizeof(double)),
+                               std::min<int64_t>(G.chunk, plan->ws_pts), &k);
         if (e != cudaSuccess)
-            return capi_cuda_fail(e, "blocks run");
+            break;
     }
-    return BNSN_OK;
+    // join even after an error, so that the caller's stream never runs ahead
+    const cudaError_t e1 = cudaEventRecord(plan->ev[1], plan->aux);
+    const cudaError_t e2 = e1 == cudaSuccess ? cudaStreamWaitEvent(st, plan->ev[1], 0) : e1;
+    if (rc)
+        return rc;
+    if (e != cudaSuccess)
+        return capi_cuda_fail(e, "blocks run");
+    return e2 == cudaSuccess ? BNSN_OK : capi_cuda_fail(e2, "blocks run");
 }
 
 int bnsn_blocks_plan_info(bnsn_blocks_plan_t plan, int group, int* nquad, int* reactions,
@@ -306,6 +330,11 @@ int bnsn_blocks_plan_destroy(bnsn_blocks_plan_t plan)
             cudaFree(G.pidx);
     if (plan->ws)
         cudaFree(plan->ws);
+    if (plan->aux)
+        cudaStreamDestroy(plan->aux);
+    for (cudaEvent_t ev : plan->ev)
+        if (ev)
+            cudaEventDestroy(ev);
     delete plan;
     return BNSN_OK;
 }

@@ -98,6 +98,12 @@ constexpr int64_t kNoAllocPoints = 4096;
 cudaError_t noalloc_scratch(int device, double** ptr);
 cudaError_t launch_grey(const OpacityLaunch& L, cudaStream_t stream, int num_sms, double* ws,
                         int64_t ws_points, cudaStream_t aux = nullptr);
+// The chunk loop of launch_grey without the stream fork and join: chunks of
+// `chunk` points, chunk k (the running counter *k, advanced per chunk) on
+// stream0 with scratch ws0 when k is even or aux is NULL, else on aux with
+// ws1.  The caller orders aux after stream0 before and joins it after.
+cudaError_t launch_grey_chunks(const OpacityLaunch& L, cudaStream_t stream0, cudaStream_t aux,
+                               int num_sms, double* ws0, double* ws1, int64_t chunk, int64_t* k);
 // Spectral opacities (phase kernels over chunks of points).  The scratch of
 // one call holds spectral_scratch_bytes(chunk, n_energies) bytes for chunks of
 // spectral_chunk_points(n_energies) points (about kSpecChunkRecords

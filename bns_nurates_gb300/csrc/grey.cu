@@ -1539,41 +1539,25 @@ cudaError_t grey_nonfinite_count(unsigned long long* count, bool reset)
     return e;
 }
 
-cudaError_t launch_grey(const OpacityLaunch& L, cudaStream_t st0, int sms, double* ws,
-                        int64_t ws_points, cudaStream_t aux)
+cudaError_t launch_grey_chunks(const OpacityLaunch& L, cudaStream_t st0, cudaStream_t aux, int sms,
+                               double* ws0, double* ws1, int64_t chunk, int64_t* k)
 {
     if (L.npts <= 0)
         return cudaSuccess;
-    if (!ws || ws_points < 1)
+    if (!ws0 || (aux && !ws1) || chunk < 1 || !k)
         return cudaErrorInvalidValue;
-    // With an auxiliary stream, consecutive chunks alternate between the
-    // caller's stream and aux, each with half of the scratch, so that the
-    // FP64-pipe phases (prelude, pair) of one chunk run beside the FP32-pipe
-    // NES phase of the other.  The caller's stream waits for aux at the end.
-    const bool two      = aux != nullptr && ws_points >= 2 && L.npts > ws_points / 2;
     // default grid: two waves of resident CTAs per phase kernel (per-point
     // work is uneven; the second wave fills the tail of the first, and the
     // other stream's kernel the tail of both).  Half a wave per stream, so
     // that both streams' kernels stay resident side by side, measured 15%
     // slower on the 256^3 all-reactions slab.
     g_grid_scale = L.grid_scale > 0. ? L.grid_scale : 2.;
-    const int64_t chunk = two ? ws_points / 2 : ws_points;
-    cudaEvent_t ev[2]   = {nullptr, nullptr};
-    if (two)
-    {
-        cudaError_t e;
-        if ((e = cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming)) != cudaSuccess ||
-            (e = cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming)) != cudaSuccess ||
-            (e = cudaEventRecord(ev[0], st0)) != cudaSuccess ||
-            (e = cudaStreamWaitEvent(aux, ev[0], 0)) != cudaSuccess)
-            return e;
-    }
     cudaError_t err = cudaSuccess;
-    int64_t k       = 0;
-    for (int64_t p0 = 0; p0 < L.npts && err == cudaSuccess; p0 += chunk, ++k)
+    for (int64_t p0 = 0; p0 < L.npts && err == cudaSuccess; p0 += chunk, ++*k)
     {
-        const cudaStream_t st = (two && (k & 1)) ? aux : st0;
-        double* const wsk     = (two && (k & 1)) ? ws + chunk * kTabWords : ws;
+        const bool odd        = aux != nullptr && (*k & 1);
+        const cudaStream_t st = odd ? aux : st0;
+        double* const wsk     = odd ? ws1 : ws0;
         const int64_t np      = (L.npts - p0) < chunk ? (L.npts - p0) : chunk;
         const int64_t wb      = (np + kWarps - 1) / kWarps;
         phase_mark(kPhPrelude, 0, st);
@@ -1633,6 +1617,35 @@ cudaError_t launch_grey(const OpacityLaunch& L, cudaStream_t st0, int sms, doubl
         phase_mark(kPhFinal, 1, st);
         err = cudaGetLastError();
     }
+    return err;
+}
+
+cudaError_t launch_grey(const OpacityLaunch& L, cudaStream_t st0, int sms, double* ws,
+                        int64_t ws_points, cudaStream_t aux)
+{
+    if (L.npts <= 0)
+        return cudaSuccess;
+    if (!ws || ws_points < 1)
+        return cudaErrorInvalidValue;
+    // With an auxiliary stream, consecutive chunks alternate between the
+    // caller's stream and aux, each with half of the scratch, so that the
+    // FP64-pipe phases (prelude, pair) of one chunk run beside the FP32-pipe
+    // NES phase of the other.  The caller's stream waits for aux at the end.
+    const bool two      = aux != nullptr && ws_points >= 2 && L.npts > ws_points / 2;
+    const int64_t chunk = two ? ws_points / 2 : ws_points;
+    cudaEvent_t ev[2]   = {nullptr, nullptr};
+    if (two)
+    {
+        cudaError_t e;
+        if ((e = cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaEventRecord(ev[0], st0)) != cudaSuccess ||
+            (e = cudaStreamWaitEvent(aux, ev[0], 0)) != cudaSuccess)
+            return e;
+    }
+    int64_t k       = 0;
+    cudaError_t err = launch_grey_chunks(L, st0, two ? aux : nullptr, sms, ws,
+                                         two ? ws + chunk * kTabWords : nullptr, chunk, &k);
     if (two)
     {
         const cudaError_t e1 = cudaEventRecord(ev[1], aux);
