@@ -910,9 +910,7 @@ __global__ void __launch_bounds__(kWarps * 32)
                 }
                 if (GUARD)
                 {
-                    // FP32 error bounds against each output's total; the first
-                    // check flags the parts above half the total, the second
-                    // every part still in FP32
+                    // FP32 error bounds against each output's total
 #pragma unroll
                     for (int kk = 0; kk < 8; ++kk)
                     {
@@ -923,17 +921,18 @@ __global__ void __launch_bounds__(kWarps * 32)
                         const double at  = fabs(tot);
                         if (!(bb + bn <= at))
                         {
+                            // the parts above half of a finite total (at least
+                            // one is); both when neither is (or the total is
+                            // not finite).  A bound is ~1e6 x the part's actual
+                            // error, so redoing one part hardly moves the total
+                            // and the kept part stays below half of it.
                             bool xp = bb > 0., xn = bn > 0.;
-                            if (MODE == kSpecMixed)
+                            const bool hp = xp && !(bb <= 0.5 * at);
+                            const bool hn = xn && !(bn <= 0.5 * at);
+                            if (hp || hn)
                             {
-                                // at least one part is above half of a finite total
-                                const bool hp = xp && !(bb <= 0.5 * at);
-                                const bool hn = xn && !(bn <= 0.5 * at);
-                                if (hp || hn)
-                                {
-                                    xp = hp;
-                                    xn = hn;
-                                }
+                                xp = hp;
+                                xn = hn;
                             }
                             fpb  = fpb || xp;
                             fnes = fnes || xn;
