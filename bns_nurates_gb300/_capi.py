@@ -158,6 +158,7 @@ SIGNATURES = {
     "bnsn_phase_times": (c_int, [P, P]),
     "bnsn_kernel_launches": (ctypes.c_int64, []),
     "bnsn_spectral_mixed_stats": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64), ctypes.c_int]),
+    "bnsn_distr_from_m1_point": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "bnsn_gp19_load_header": (ctypes.c_int, [ctypes.c_char_p]),
     "bnsn_nonfinite_outputs": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64), ctypes.c_int]),
     "bnsn_status_string": (ctypes.c_char_p, [c_int]),

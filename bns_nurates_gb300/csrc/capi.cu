@@ -854,6 +854,59 @@ extern "C" int bnsn_compute_m1_opacities_point(const MyQuadrature* quad_1d,
     return BNSN_OK;
 }
 
+extern "C" int bnsn_distr_from_m1_point(const M1Quantities* m1, NuDistributionParams* out)
+{
+    g_err.clear();
+    if (!m1 || !out)
+        return fail(BNSN_ERR_ARG, "m1/out is NULL");
+    DeviceState* st;
+    int rc = device_state(&st);
+    if (rc)
+        return rc;
+    std::lock_guard<std::mutex> lk(g_stage_mu);
+    double* buf;
+    if ((rc = stage(st, sizeof(double) * (12 + 28), &buf)))
+        return rc;
+    double h[12];
+    for (int s = 0; s < 4; ++s)
+    {
+        h[s]     = m1->n[s];
+        h[4 + s] = m1->J[s];
+        h[8 + s] = m1->chi[s];
+    }
+    cudaStream_t s0 = st->streams[0];
+    cudaError_t err = cudaMemcpyAsync(buf, h, sizeof(h), cudaMemcpyHostToDevice, s0);
+    if (err != cudaSuccess)
+        return cuda_fail(err, "cudaMemcpyAsync");
+    bnsn_m1_soa Mq;
+    bnsn_distr_soa D;
+    double* db = buf + 12; // NuDistributionParams field order, 7 x 4
+    for (int s = 0; s < 4; ++s)
+    {
+        Mq.n[s]     = buf + s;
+        Mq.J[s]     = buf + 4 + s;
+        Mq.chi[s]   = buf + 8 + s;
+        D.w_t[s]    = db + s;
+        D.temp_t[s] = db + 4 + s;
+        D.eta_t[s]  = db + 8 + s;
+        D.w_f[s]    = db + 12 + s;
+        D.temp_f[s] = db + 16 + s;
+        D.c_f[s]    = db + 20 + s;
+        D.beta_f[s] = db + 24 + s;
+    }
+    if ((rc = bnsn_distr_from_m1(&Mq, &D, 1, s0)))
+        return rc;
+    double o[28];
+    err = cudaMemcpyAsync(o, db, sizeof(o), cudaMemcpyDeviceToHost, s0);
+    if (err == cudaSuccess)
+        err = cudaStreamSynchronize(s0);
+    if (err != cudaSuccess)
+        return cuda_fail(err, "point result copy");
+    static_assert(sizeof(NuDistributionParams) == sizeof(o), "NuDistributionParams layout");
+    memcpy(out, o, sizeof(o));
+    return BNSN_OK;
+}
+
 extern "C" int bnsn_compute_spectral_opacities_point(double nu, const MyQuadrature* quad_1d,
                                                      const GreyOpacityParams* gp,
                                                      int stimulated, SpectralOpacities* out)

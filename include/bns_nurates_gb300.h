@@ -410,6 +410,10 @@ int bnsn_compute_m1_opacities_point(const MyQuadrature* quad_1d,
                                     const GreyOpacityParams* grey_pars,
                                     int stim_abs, M1Opacities* out);
 
+/* One point; same as CalculateDistrParamsFromM1(m1_pars, eos_pars)
+ * (distribution.hpp:323-333, which does not read eos_pars). */
+int bnsn_distr_from_m1_point(const M1Quantities* m1, NuDistributionParams* out);
+
 /* One point, one energy; same as ComputeSpectralOpacities{Not,}StimulatedAbs
  * (m1_opacities.hpp:1506-1660). */
 int bnsn_compute_spectral_opacities_point(double nu, const MyQuadrature* quad_1d,
