@@ -8,6 +8,7 @@
 #include <math.h>
 
 #include "bnsn_constants.h"
+#include "bnsn_df.cuh"
 #include "bnsn_fp64.cuh"
 
 namespace bnsn {
@@ -16,31 +17,39 @@ namespace fp32 {
 #define BNSN_DI __device__ __forceinline__
 
 // HR98 bremsstrahlung (kernel_brem_HR98.hpp:33-338) split into per-point FP64
-// constants (below, rounded to FP32) and an FP32 shape of x = (w + w')/T:
+// constants (below, rounded to FP32 or kept as double-float) and an FP32
+// shape of x = (w + w')/T:
 //   s_abs(x) = outer * sum_ch pre_ch * S_ch(x) / (x^2 + hgg_ch^2)
 // with outer = 3 C_brem / medium correction and pre_ch = n_ch gamma_ch / T.
+// The non-degenerate part s_nd (Eq. 45: a ratio of powers up to x^4) and the
+// factors x (x^2 + 4 pi^2) / (1 - e^-x) of s_d run in double-float from the
+// double-float x: in FP32 their rounding (and that of x itself, amplified up
+// to 4x by q^4) reached 8.5e-7 of the shape.
 struct Hr98Mixed
 {
-    float y, ey12, poly_y, y4p1, Dy, p, pinv;
-    float K1[3], f_u[3], eta2p1[3], sqe[3], ep2[3], h[3], hgg2[3], pre[3];
+    float y, poly_y, y4p1, Dy, p, pinv;
+    float K1fu[3], eta2p1[3], sqe[3], ep2[3], h[3], hgg2[3], pre[3];
+    dfm::df cX, cq, cp, y2; // 2 - e^{-y/12}, pi^(1/8) + y, 5 y^2 / 3 + 1, 2 y
     double outer;
 };
 
 BNSN_DI void hr98_mixed_from(const fp64::Hr98Point& P, Hr98Mixed* M)
 {
     M->y      = (float)P.y;
-    M->ey12   = (float)P.ey12;
     M->poly_y = (float)P.poly_y;
     M->y4p1   = (float)P.y4p1;
     M->Dy     = (float)P.Dy;
     M->p      = (float)(-P.mp);
     M->pinv   = (float)(-P.minv);
+    M->cX     = dfm::from_double(2. - P.ey12);
+    M->cq     = dfm::from_double(k::Pi18 + P.y);
+    M->cp     = dfm::from_double(P.poly_y + 1.);
+    M->y2     = dfm::from_double(2. * P.y);
 #pragma unroll
     for (int c = 0; c < 3; ++c)
     {
         const fp64::Hr98Channel& C = P.ch[c];
-        M->K1[c]     = (float)C.K1;
-        M->f_u[c]    = (float)C.f_u;
+        M->K1fu[c]   = (float)(C.K1 * C.f_u / k::FourPiSq);
         M->eta2p1[c] = (float)C.eta2p1;
         M->sqe[c]    = (float)C.sqe;
         M->ep2[c]    = (float)C.ep2;
@@ -68,21 +77,34 @@ BNSN_DI float powf_acc(float x, float p)
     return ldexpf(exp2f(f), (int)n);
 }
 
-// Sum over the three NN channels of n gamma S(x) / (T (x^2 + (gamma g/2)^2)).
-// The interpolation (s_nd^-p + s_d^-p)^(-1/p) of Eq.(49) is evaluated as
-// min * (1 + (max/min)^-p)^(-1/p): the same value, but the outer power acts on
-// a number in [1, 2], which keeps its FP32 rounding error at the ulp level
-// instead of growing with |p log s|.
-BNSN_DI float hr98_shape(const Hr98Mixed& M, float x_in)
+// Sum over the three NN channels of n gamma S(x) / (T (x^2 + (gamma g/2)^2))
+// at x = xh + xl (double-float).  The interpolation (s_nd^-p + s_d^-p)^(-1/p)
+// of Eq.(49) is evaluated as min * (1 + (max/min)^-p)^(-1/p): the same value,
+// but the outer power acts on a number in [1, 2], which keeps its FP32
+// rounding error at the ulp level instead of growing with |p log s|.
+BNSN_DI float hr98_shape(const Hr98Mixed& M, float xh_in, float xl_in)
 {
-    const float x   = fmaxf(x_in, (float)k::BremXmin);
-    const float y   = M.y;
-    const float X   = x + 2.f - M.ey12;
-    const float q   = (float)k::Pi18 + x + y;
-    const float snd = 2.f * (float)k::SqrtPi * (X * sqrtf(X)) * (x * x + 2.f * x * y + M.poly_y + 1.f) /
-                      ((float)k::SqrtPi + (q * q) * (q * q));
-    const float em1 = -expm1f(-x);
-    const float X2  = x * x + (float)k::FourPiSq;
+    using namespace dfm;
+    constexpr dfc kSqrtPi(k::SqrtPi), kTwoSqrtPi(2. * k::SqrtPi), kFourPiSq(k::FourPiSq);
+    const bool clamp = xh_in < (float)k::BremXmin;
+    const df X1      = clamp ? mk((float)k::BremXmin) : df{xh_in, xl_in}; // x clamped
+    const float x    = X1.hi;
+    const float y    = M.y;
+    // s_nd = 2 sqrt(pi) X^1.5 (x^2 + 2 x y + 5 y^2 / 3 + 1) / (sqrt(pi) + q^4)
+    const df Xd   = add(X1, M.cX);                       // X = x + 2 - e^{-y/12}
+    const float sx = sqrtf(Xd.hi);
+    const df sX   = {sx, (fmaf(-sx, sx, Xd.hi) + Xd.lo) / (2.f * sx)}; // sqrt(X), one Newton step
+    const df poly = add(mul(X1, add(X1, M.y2)), M.cp);
+    const df q    = add(X1, M.cq);
+    const df q2   = mul(q, q);
+    const df den  = add(mul(q2, q2), mk(kSqrtPi));
+    const df sndd = div(mul(mul(mul(Xd, sX), poly), mk(kTwoSqrtPi)), den);
+    const float snd = sndd.hi + sndd.lo;
+    // x (x^2 + 4 pi^2) / (1 - e^-x) of s_d
+    const float ex   = expf(-x);
+    const float em1  = -expm1f(-x) + ex * X1.lo;
+    const df X2x     = mul(add(mul(X1, X1), mk(kFourPiSq)), X1);
+    const float sdx  = (X2x.hi + X2x.lo) / em1;
     const float px11  = powf_acc(x, 1.1f);
     const float px093 = powf_acc(x, 0.93f);
     const float px12  = powf_acc(x, 1.2f);
@@ -91,12 +113,14 @@ BNSN_DI float hr98_shape(const Hr98Mixed& M, float x_in)
     const float xterm = 3.f + (x - 1.2f) * (x - 1.2f) + 1.f / (x2 * x2);
     const float gpart = 0.0044f * px11 * y / M.Dy;
     const float cden2 = 30.f + 0.005f * px28;
-    const float xs2   = x_in * x_in;
+    const df XS       = {xh_in, xl_in}; // x unclamped, as the reference's x^2
+    const df xs2d     = mul(XS, XS);
+    const float xs2   = xs2d.hi + xs2d.lo;
     float tot         = 0.f;
 #pragma unroll
     for (int c = 0; c < 3; ++c)
     {
-        const float s_d    = M.K1[c] * X2 * x * M.f_u[c] / ((float)k::FourPiSq * em1);
+        const float s_d    = M.K1fu[c] * sdx;
         const float lo     = fminf(snd, s_d);
         const float hi     = fmaxf(snd, s_d);
         const float t      = powf_acc(hi / lo, -M.p);

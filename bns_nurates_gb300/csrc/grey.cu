@@ -402,7 +402,7 @@ struct CellTab32
 struct Acc32
 {
     float v[16];
-    float mag[8]; // sum of |term| of the number moments (em, ab per species)
+    float mag[16]; // sum of |term| per moment
     __device__ __forceinline__ void clear()
     {
 #pragma unroll
@@ -411,23 +411,60 @@ struct Acc32
     }
 };
 
-// Largest error amplification of the number moments of a point: the sum of
-// |term| over |total|, where the total adds the other reactions' sums of the
-// same output (`other`, already in the units of scale x acc; nullptr: none).
-// Terms are those of this lane (acc, mag, unscaled); the result is
+// Largest error amplification over the 16 moments of a point (number and
+// energy, emission and absorption, 4 species): the sum of |term| over
+// |total|, where the total adds the other reactions' sums of the same output
+// (`other`, in the units of scale x acc: the pair, brem or NES sums already
+// computed and the beta rates, which cancel the brem or NES sums where the
+// reconstructed occupation exceeds 1).  Terms are those of this lane (acc,
+// mag, unscaled; moments 8..15 scaled by scale_e); the result is
 // warp-reduced and 1 when every contribution has one sign.
 __device__ __forceinline__ double cancel_factor(const double* acc, const float* mag, double scale,
-                                                const double* other)
+                                                double scale_e, const double* other)
 {
     double amp = 1.;
 #pragma unroll
-    for (int s = 0; s < 8; ++s)
+    for (int s = 0; s < 16; ++s)
     {
-        const double m   = warp_sum((double)mag[s]) * scale;
-        const double tot = fabs(warp_sum(acc[s]) * scale + (other ? other[s] : 0.));
+        const double sc  = s < 8 ? scale : scale_e;
+        const double m   = warp_sum((double)mag[s]) * sc;
+        const double tot = fabs(warp_sum(acc[s]) * sc + other[s]);
         amp = fmax(amp, m > 0. ? m / tot : 1.);
     }
     return amp;
+}
+
+// The beta rates of a point in the units of the pair/brem sums (s2d, unit
+// t2 = (2.182 T)^2 for number and t2d t2 for energy moments) or, with
+// to_nes, of the NES sums (unit hn = 8 t2, times T for energy moments), as
+// the final assembly combines them (m1_opacities.hpp:1172-1294).
+__device__ __forceinline__ void beta_in_sum_units(const PointTab* P, double T, double eta_e,
+                                                  bool use_abs_em, bool to_nes, double* b)
+{
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk)
+        b[kk] = 0.;
+    if (!use_abs_em)
+        return;
+    double fe[2][6];
+#pragma unroll
+    for (int e = 0; e < 2; ++e)
+#pragma unroll
+        for (int kk = 0; kk < 6; ++kk)
+            fe[e][kk] = P->fe[e][kk];
+    double sb[2];
+    beta_scales(T, eta_e, fe, sb);
+    const double t2d = k::TempMultiple * T, t2 = t2d * t2d;
+    const double un  = k::FourPiHc3 * (to_nes ? 8. * t2 : t2);
+    const double ue  = to_nes ? un : un * t2d;
+#pragma unroll
+    for (int s = 0; s < 2; ++s)
+    {
+        b[s]      = P->sbeta[s] * sb[s] / un;     // number emission
+        b[4 + s]  = P->sbeta[4 + s] * sb[s] / un; // number absorption
+        b[8 + s]  = P->sbeta[2 + s] * sb[s] / ue; // energy emission
+        b[12 + s] = P->sbeta[6 + s] * sb[s] / ue; // energy absorption
+    }
 }
 
 // Mixed sums whose terms cancel by more than this are recomputed in FP64: the
@@ -439,12 +476,13 @@ constexpr double kMaxCancelBrem = 1.25;
 constexpr double kMaxCancelDf = 1e5;
 
 // add_cell in FP32 for a species-independent kernel (brem): K_em, K_ab are
-// dimensionless, w4 = (y_a y_b)^2; the caller scales by T^4 and the kernel's
-// prefactor.
+// dimensionless; P1 = (y_a y_b)^2 W1 and P2 = (y_a y_b)^2 W2 are the cell's
+// weights with the energy factor, each one FP32 rounding of a double-float
+// product (cell_weight); the caller scales by T^4 and the kernel's prefactor.
 template <bool STIM>
 __device__ __forceinline__ void add_cell32(Acc32& A, float Kem, float Kab, const float* ga,
                                            const float* gma, const float* gb, const float* gmb,
-                                           bool nb_block, float w4, float W1, float W2)
+                                           bool nb_block, float P1, float P2)
 {
 #pragma unroll
     for (int s = 0; s < 4; ++s)
@@ -455,21 +493,33 @@ __device__ __forceinline__ void add_cell32(Acc32& A, float Kem, float Kab, const
         float EM, AB;
         if (STIM)
         {
-            AB = w4 * ga[s] * (em + am);
-            EM = em * w4;
+            AB = ga[s] * (em + am);
+            EM = em;
         }
         else
         {
-            AB = am * (w4 * ga[s]);
-            EM = em * (w4 * gma[s]);
+            AB = am * ga[s];
+            EM = em * gma[s];
         }
-        A.v[s] += EM * W1;
-        A.v[4 + s] += AB * W1;
-        A.v[8 + s] += EM * W2;
-        A.v[12 + s] += AB * W2;
-        A.mag[s] += fabsf(EM * W1);
-        A.mag[4 + s] += fabsf(AB * W1);
+        const float e1 = EM * P1, a1 = AB * P1;
+        A.v[s] += e1;
+        A.v[4 + s] += a1;
+        const float e2 = EM * P2, a2 = AB * P2;
+        A.v[8 + s] += e2;
+        A.v[12 + s] += a2;
+        A.mag[s] += fabsf(e1);
+        A.mag[4 + s] += fabsf(a1);
+        A.mag[8 + s] += fabsf(e2);
+        A.mag[12 + s] += fabsf(a2);
     }
+}
+
+// (y_a y_b)^2 w_a w_b rounded once to FP32 from double-float factors (in
+// FP32 the fourth power alone magnified the rounding of y to 3e-7).
+__device__ __forceinline__ float cell_weight(dfm::df w4, dfm::df wa, dfm::df wb)
+{
+    const dfm::df p = dfm::mul(w4, dfm::mul(wa, wb));
+    return p.hi + p.lo;
 }
 
 // FP32 tables of one point from the FP64 ones.
@@ -495,7 +545,6 @@ __global__ void __launch_bounds__(kWarps * 32)
                      double* __restrict__ scratch)
 {
     __shared__ double s_A1[kMaxM], s_A2[kMaxM];
-    __shared__ float s_A1f[kMaxM], s_A2f[kMaxM];
     __shared__ uint32_t s_cells[kMaxCells];
     __shared__ CellTab s_ct[kWarps];
     __shared__ CellTab32 s_c32[MIXED ? kWarps : 1];
@@ -503,8 +552,6 @@ __global__ void __launch_bounds__(kWarps * 32)
     {
         s_A1[k]  = L.A1[k];
         s_A2[k]  = L.A2[k];
-        s_A1f[k] = (float)L.A1[k];
-        s_A2f[k] = (float)L.A2[k];
     }
     for (int k = threadIdx.x; k < L.ncell; k += blockDim.x)
         s_cells[k] = L.cells[k];
@@ -588,7 +635,7 @@ __global__ void __launch_bounds__(kWarps * 32)
                      double* __restrict__ scratch, int add)
 {
     __shared__ double s_A1[kMaxM], s_A2[kMaxM];
-    __shared__ float s_A1f[kMaxM], s_A2f[kMaxM];
+    __shared__ dfm::df s_A1d[MIXED ? kMaxM : 1], s_A2d[MIXED ? kMaxM : 1];
     __shared__ uint32_t s_cells[kMaxCells];
     __shared__ CellTab s_ct[kWarps];
     __shared__ CellTab32 s_c32[MIXED ? kWarps : 1];
@@ -600,10 +647,13 @@ __global__ void __launch_bounds__(kWarps * 32)
     const bool prof = IMPL == 2 && G19.d3 <= kGp19MaxW;
     for (int k = threadIdx.x; k < kMaxM; k += blockDim.x)
     {
-        s_A1[k]  = L.A1[k];
-        s_A2[k]  = L.A2[k];
-        s_A1f[k] = (float)L.A1[k];
-        s_A2f[k] = (float)L.A2[k];
+        s_A1[k] = L.A1[k];
+        s_A2[k] = L.A2[k];
+        if (MIXED)
+        {
+            s_A1d[k] = dfm::from_double(L.A1[k]);
+            s_A2d[k] = dfm::from_double(L.A2[k]);
+        }
     }
     for (int k = threadIdx.x; k < L.ncell; k += blockDim.x)
         s_cells[k] = L.cells[k];
@@ -679,7 +729,7 @@ __global__ void __launch_bounds__(kWarps * 32)
             Acc32 A;
             A.clear();
 #pragma unroll
-            for (int kk = 0; kk < 8; ++kk)
+            for (int kk = 0; kk < 16; ++kk)
                 A.mag[kk] = 0.f;
             int pending = 0;
             for (int c = lane; c < L.ncell; c += 32)
@@ -692,7 +742,7 @@ __global__ void __launch_bounds__(kWarps * 32)
                 float Kab;
                 bool slow = false;
                 if (IMPL == 0)
-                    Kab = fp32::hr98_shape(C.hm, xs.hi);
+                    Kab = fp32::hr98_shape(C.hm, xs.hi, xs.lo);
                 else
                 {
                     float wv = (float)(C.nu[a] + C.nu[b]);
@@ -726,23 +776,23 @@ __global__ void __launch_bounds__(kWarps * 32)
                     Kab = (float)(abv / (3. * GW.pt.C));
                     Kem = (float)(em / (3. * GW.pt.C));
                 }
-                const float ya = D.yh[a], yb = D.yh[b];
-                const float w4 = (ya * ya) * (yb * yb);
-                const float W1 = s_A1f[a] * s_A1f[b];
+                const dfm::df yab = dfm::mul(dfm::df{D.yh[a], D.yl[a]}, dfm::df{D.yh[b], D.yl[b]});
+                const dfm::df w4  = dfm::mul(yab, yab); // (y_a y_b)^2
+                const float P1    = cell_weight(w4, s_A1d[a], s_A1d[b]);
+                const float P2    = cell_weight(w4, s_A2d[a], s_A1d[b]);
                 if (L.stim)
-                    add_cell32<true>(A, Kem, Kab, D.g[a], D.gm[a], D.g[b], D.gm[b], nbb, w4, W1,
-                                     s_A2f[a] * s_A1f[b]);
+                    add_cell32<true>(A, Kem, Kab, D.g[a], D.gm[a], D.g[b], D.gm[b], nbb, P1, P2);
                 else
-                    add_cell32<false>(A, Kem, Kab, D.g[a], D.gm[a], D.g[b], D.gm[b], nbb, w4, W1,
-                                      s_A2f[a] * s_A1f[b]);
+                    add_cell32<false>(A, Kem, Kab, D.g[a], D.gm[a], D.g[b], D.gm[b], nbb, P1, P2);
                 if (a != b)
                 {
+                    const float P2r = cell_weight(w4, s_A2d[b], s_A1d[a]);
                     if (L.stim)
-                        add_cell32<true>(A, Kem, Kab, D.g[b], D.gm[b], D.g[a], D.gm[a], nbb, w4,
-                                         W1, s_A2f[b] * s_A1f[a]);
+                        add_cell32<true>(A, Kem, Kab, D.g[b], D.gm[b], D.g[a], D.gm[a], nbb, P1,
+                                         P2r);
                     else
-                        add_cell32<false>(A, Kem, Kab, D.g[b], D.gm[b], D.g[a], D.gm[a], nbb, w4,
-                                          W1, s_A2f[b] * s_A1f[a]);
+                        add_cell32<false>(A, Kem, Kab, D.g[b], D.gm[b], D.g[a], D.gm[a], nbb, P1,
+                                          P2r);
                 }
                 if (++pending == 4)
                 {
@@ -757,12 +807,14 @@ __global__ void __launch_bounds__(kWarps * 32)
             for (int kk = 0; kk < 16; ++kk)
                 acc[kk] = acc[kk] + (double)A.v[kk];
             // cells of both signs (occupation above 1 makes 1 - g negative), or
-            // a brem sum cancelling the pair sum: recompute this point in FP64
-            double pair_n[8];
+            // a brem sum cancelling the pair sum or the beta rates: recompute
+            // this point in FP64
+            double other[16];
+            beta_in_sum_units(P, T, L.eos[7][p] / T, L.use_abs_em, false, other);
 #pragma unroll
-            for (int kk = 0; kk < 8; ++kk)
-                pair_n[kk] = add ? P->s2d[kk] : 0.;
-            redo = cancel_factor(acc, A.mag, scale, pair_n) > kMaxCancelBrem;
+            for (int kk = 0; kk < 16; ++kk)
+                other[kk] += add ? P->s2d[kk] : 0.;
+            redo = cancel_factor(acc, A.mag, scale, scale, other) > kMaxCancelBrem;
 #pragma unroll
             for (int kk = 0; kk < 16; ++kk)
                 acc[kk] = redo ? 0. : acc[kk] * scale;
@@ -1252,9 +1304,9 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
 #pragma unroll
                 for (int kk = 0; kk < 16; ++kk)
                     dacc[kk] = {0.f, 0.f};
-                float mag[8];
+                float mag[16];
 #pragma unroll
-                for (int kk = 0; kk < 8; ++kk)
+                for (int kk = 0; kk < 16; ++kk)
                     mag[kk] = 0.f;
                 const int nn2 = n2 * n2;
                 for (int it = lane; it < 2 * nn2; it += 32)
@@ -1303,12 +1355,16 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
                                 EM2 = w4 * gbm[s] * e2;
                             }
                             const float tem = Wf * (EM1 + EM2), tab = Wf * (AB1 + AB2);
+                            const float tee = Wf * (fw * EM1 + fwp * EM2);
+                            const float tae = Wf * (fw * AB1 + fwp * AB2);
                             dacc[s]      = dfm::add(dacc[s], tem);
                             dacc[4 + s]  = dfm::add(dacc[4 + s], tab);
-                            dacc[8 + s]  = dfm::add(dacc[8 + s], Wf * (fw * EM1 + fwp * EM2));
-                            dacc[12 + s] = dfm::add(dacc[12 + s], Wf * (fw * AB1 + fwp * AB2));
+                            dacc[8 + s]  = dfm::add(dacc[8 + s], tee);
+                            dacc[12 + s] = dfm::add(dacc[12 + s], tae);
                             mag[s] += fabsf(tem);
                             mag[4 + s] += fabsf(tab);
+                            mag[8 + s] += fabsf(tee);
+                            mag[12 + s] += fabsf(tae);
                         }
                     }
                     else
@@ -1351,12 +1407,16 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
                                 EM2 = mul(mul(w4, gbm[s]), e2);
                             }
                             const df tem = mul(Wd, add(EM1, EM2)), tab = mul(Wd, add(AB1, AB2));
+                            const df tee = mul(Wd, add(mul(W, EM1), mul(WP, EM2)));
+                            const df tae = mul(Wd, add(mul(W, AB1), mul(WP, AB2)));
                             dacc[s]      = add(dacc[s], tem);
                             dacc[4 + s]  = add(dacc[4 + s], tab);
-                            dacc[8 + s]  = add(dacc[8 + s], mul(Wd, add(mul(W, EM1), mul(WP, EM2))));
-                            dacc[12 + s] = add(dacc[12 + s], mul(Wd, add(mul(W, AB1), mul(WP, AB2))));
+                            dacc[8 + s]  = add(dacc[8 + s], tee);
+                            dacc[12 + s] = add(dacc[12 + s], tae);
                             mag[s] += fabsf(tem.hi);
                             mag[4 + s] += fabsf(tab.hi);
+                            mag[8 + s] += fabsf(tee.hi);
+                            mag[12 + s] += fabsf(tae.hi);
                         }
                     }
                 }
@@ -1365,14 +1425,19 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
                     acc[kk] = dfm::to_double(dacc[kk]);
                 // terms of both signs (occupation above 1), or NES sums
                 // cancelling the pair + brem sums of the same output (those enter
-                // the assembly with t2d^2 = hn / 8): the fast pass hands the point
-                // to the accurate pass, the accurate pass to FP64
+                // the assembly with t2d^2 = hn / 8, times t2d for energy moments)
+                // or the beta rates: the fast pass hands the point to the
+                // accurate pass, the accurate pass to FP64
                 const double T4 = (T * T) * (T * T);
-                double other[8];
+                double other[16];
+                beta_in_sum_units(P, T, NP.eta0, L.use_abs_em, true, other);
+                const double t2d = k::TempMultiple * T;
 #pragma unroll
-                for (int kk = 0; kk < 8; ++kk)
-                    other[kk] = (L.use_pair || L.use_brem) ? 0.125 * P->s2d[kk] : 0.;
-                const double amp = cancel_factor(acc, mag, NP.pre * T4, other);
+                for (int kk = 0; kk < 16; ++kk)
+                    other[kk] += (L.use_pair || L.use_brem)
+                                     ? 0.125 * P->s2d[kk] * (kk >= 8 ? t2d : 1.)
+                                     : 0.;
+                const double amp = cancel_factor(acc, mag, NP.pre * T4, NP.pre * T4 * T, other);
                 if (amp > (MODE == kNesFast ? kMaxCancel : kMaxCancelDf))
                     flag = MODE == kNesFast ? 1 : 2;
 #pragma unroll

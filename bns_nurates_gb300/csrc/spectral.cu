@@ -223,6 +223,7 @@ template <int MODE>
 struct PbShared
 {
     double x[kMaxQ], B1[kMaxM];
+    dfm::df B1d[kMaxM]; // mixed: weights as double-float
     double lw[kGp19MaxW];
     float lwf[kGp19MaxW];
     PbWarp w[kWarps];
@@ -262,7 +263,10 @@ __global__ void __launch_bounds__(kWarps * 32)
     for (int k = threadIdx.x; k < kMaxQ; k += blockDim.x)
         S.x[k] = L.x1[k];
     for (int k = threadIdx.x; k < kMaxM; k += blockDim.x)
-        S.B1[k] = L.B1[k];
+    {
+        S.B1[k]  = L.B1[k];
+        S.B1d[k] = dfm::from_double(L.B1[k]);
+    }
     if (prof)
         for (int k = threadIdx.x; k < G19.d3; k += blockDim.x)
         {
@@ -478,7 +482,7 @@ __global__ void __launch_bounds__(kWarps * 32)
                             float kab;
                             bool slow = false;
                             if (L.brem_impl == 0)
-                                kab = fp32::hr98_shape(X.hm, xs.hi);
+                                kab = fp32::hr98_shape(X.hm, xs.hi, xs.lo);
                             else
                             {
                                 float wv = (float)(nu + nub);
@@ -512,7 +516,10 @@ __global__ void __launch_bounds__(kWarps * 32)
                                 kab = (float)(abv / (3. * W.gp.C));
                                 kem = (float)(em * exp(w) / (3. * W.gp.C));
                             }
-                            const float wy2 = (float)wa * (X.ybh[a] * X.ybh[a]);
+                            // w nubar^2 / T^2 rounded once from double-float factors
+                            const dfm::df yb  = {X.ybh[a], X.ybl[a]};
+                            const dfm::df wyd = dfm::mul(S.B1d[a], dfm::mul(yb, yb));
+                            const float wy2   = wyd.hi + wyd.lo;
 #pragma unroll
                             for (int s = 0; s < 4; ++s)
                             {
