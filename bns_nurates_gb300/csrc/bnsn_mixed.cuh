@@ -26,6 +26,24 @@ __device__ __forceinline__ int bracket_sorted(R lw, const R* ax, int d3, R* t)
     return lo;
 }
 
+// Interval of w on the GP19 w axis and its interpolation weight in FP32, for
+// an FP64 w already clipped to the axis.  The interval comes from an FP32
+// search of log w; the weight from log1p of the offset to the interval's first
+// node, (w - w_l) / w_l, so that it keeps the relative precision of that
+// offset: logf(w) itself is off by up to an ulp of log w (~5e-7 at w ~ 400
+// MeV), which moved the weight by 1e-6 and the brem cell by up to 1.4e-6.
+// wax, iw: the axis and 1 / axis (FP64); lwf: log axis (FP32); idl:
+// 1 / (log w_{l+1} - log w_l) (FP32).
+__device__ __forceinline__ int gp19_bracket32(double w, const float* lwf, const double* wax,
+                                              const double* iw, const float* idl, int d3,
+                                              float* tw)
+{
+    float t;
+    const int l = bracket_sorted<float>(logf((float)w), lwf, d3, &t);
+    *tw         = log1pf((float)((w - wax[l]) * iw[l])) * idl[l];
+    return l;
+}
+
 // Per-point data of the mixed item loop.
 struct NepsMixed
 {

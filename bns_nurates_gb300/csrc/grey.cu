@@ -642,6 +642,9 @@ __global__ void __launch_bounds__(kWarps * 32)
     __shared__ Gp19Warp s_gw[IMPL == 2 ? kWarps : 1];
     __shared__ double s_lw[IMPL == 2 ? kGp19MaxW : 1];
     __shared__ float s_lwf[IMPL == 2 ? kGp19MaxW : 1];
+    constexpr int kWF = (IMPL == 2 && MIXED) ? kGp19MaxW : 1;
+    __shared__ double s_wax[kWF], s_iw[kWF];
+    __shared__ float s_idl[kWF];
     const Gp19Table G19 = {L.gp19.d0, L.gp19.d1, L.gp19.d2,    L.gp19.d3,   L.gp19.nb,  L.gp19.ye,
                            L.gp19.t,  L.gp19.w,  L.gp19.lognb, L.gp19.logw, L.gp19.data};
     const bool prof = IMPL == 2 && G19.d3 <= kGp19MaxW;
@@ -662,6 +665,12 @@ __global__ void __launch_bounds__(kWarps * 32)
         {
             s_lw[k]  = G19.logw[k];
             s_lwf[k] = (float)G19.logw[k];
+            if (MIXED)
+            {
+                s_wax[k] = G19.w[k];
+                s_iw[k]  = 1. / G19.w[k];
+                s_idl[k] = k + 1 < G19.d3 ? (float)(1. / (G19.logw[k + 1] - G19.logw[k])) : 0.f;
+            }
         }
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -745,10 +754,10 @@ __global__ void __launch_bounds__(kWarps * 32)
                     Kab = fp32::hr98_shape(C.hm, xs.hi, xs.lo);
                 else
                 {
-                    float wv = (float)(C.nu[a] + C.nu[b]);
-                    wv       = fminf(fmaxf(wv, (float)wmin), (float)wmax);
+                    double wv = C.nu[a] + C.nu[b];
+                    wv        = wv > wmax ? wmax : (wv < wmin ? wmin : wv);
                     float tw;
-                    const int l = bracket_sorted<float>(logf(wv), s_lwf, G19.d3, &tw);
+                    const int l = gp19_bracket32(wv, s_lwf, s_wax, s_iw, s_idl, G19.d3, &tw);
                     const float v0 = GW.pf[0][l] + tw * (GW.pf[0][l + 1] - GW.pf[0][l]);
                     if (GW.pt.regime <= 1)
                         Kab = v0;

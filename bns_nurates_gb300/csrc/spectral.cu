@@ -224,8 +224,8 @@ struct PbShared
 {
     double x[kMaxQ], B1[kMaxM];
     dfm::df B1d[kMaxM]; // mixed: weights as double-float
-    double lw[kGp19MaxW];
-    float lwf[kGp19MaxW];
+    double lw[kGp19MaxW], wax[kGp19MaxW], iw[kGp19MaxW];
+    float lwf[kGp19MaxW], idl[kGp19MaxW];
     PbWarp w[kWarps];
     PbWarpMixed m[MODE == kSpecMixed ? kWarps : 1];
 };
@@ -272,6 +272,9 @@ __global__ void __launch_bounds__(kWarps * 32)
         {
             S.lw[k]  = G19.logw[k];
             S.lwf[k] = (float)G19.logw[k];
+            S.wax[k] = G19.w[k];
+            S.iw[k]  = 1. / G19.w[k];
+            S.idl[k] = k + 1 < G19.d3 ? (float)(1. / (G19.logw[k + 1] - G19.logw[k])) : 0.f;
         }
     __syncthreads();
 
@@ -485,11 +488,11 @@ __global__ void __launch_bounds__(kWarps * 32)
                                 kab = fp32::hr98_shape(X.hm, xs.hi, xs.lo);
                             else
                             {
-                                float wv = (float)(nu + nub);
-                                wv       = fminf(fmaxf(wv, (float)wmin), (float)wmax);
+                                double wv = nu + nub;
+                                wv        = wv > wmax ? wmax : (wv < wmin ? wmin : wv);
                                 float tw;
-                                const int l =
-                                    bracket_sorted<float>(logf(wv), S.lwf, G19.d3, &tw);
+                                const int l = gp19_bracket32(wv, S.lwf, S.wax, S.iw, S.idl,
+                                                             G19.d3, &tw);
                                 const float v0 =
                                     X.gp32[0][l] + tw * (X.gp32[0][l + 1] - X.gp32[0][l]);
                                 if (W.gp.regime <= 1)
