@@ -10,7 +10,8 @@ from ._capi import (BREM_BRT06, BREM_GP19, BREM_HR98, FP64, MIXED,  # noqa: F401
                     NuDistributionParams, OpacityFlags, OpacityParams, SpectralOpacities)
 from .api import (BlocksPlan, BnsnError, ComputeM1Opacities, ComputeM1OpacitiesNotStimulated,  # noqa: F401
                   ComputeSpectralOpacitiesNotStimulatedAbs,
-                  ComputeSpectralOpacitiesStimulatedAbs, distr_from_m1, flags_tuple,
+                  ComputeSpectralOpacitiesStimulatedAbs, FDI_NAMES, distr_from_m1, fdi,
+                  fdi_host, flags_tuple,
                   fp32_peak_tflops, fp64_peak_tflops, gauss_legendre, gp19_table_from_header,
                   kernel_launches, load_gp19_header, m1_opacities,
                   m1_opacities_host, nonfinite_outputs, nu_equilibrium, opacity_flags, opacity_params, params_tuple,

@@ -161,6 +161,8 @@ SIGNATURES = {
     "bnsn_distr_from_m1_point": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "bnsn_gp19_load_header": (ctypes.c_int, [ctypes.c_char_p]),
     "bnsn_nonfinite_outputs": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64), ctypes.c_int]),
+    "bnsn_fdi": (c_int, [c_int, P, P, ctypes.c_int64, P]),
+    "bnsn_fdi_host": (c_int, [c_int, P, P, ctypes.c_int64]),
     "bnsn_status_string": (ctypes.c_char_p, [c_int]),
     "bnsn_last_error": (ctypes.c_char_p, []),
     "bnsn_version": (c_int, []),

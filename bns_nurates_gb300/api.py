@@ -205,6 +205,48 @@ def nu_equilibrium(eos, stream=None):
     return distr, m1
 
 
+# Reference names of the Fermi-Dirac integral family (functions.hpp:442-4375)
+# by twice the order.
+FDI_NAMES = {-9: "FDI_m92", -7: "FDI_m72", -5: "FDI_m52", -3: "FDI_m32", -1: "FDI_m12",
+             0: "FDI_0", 1: "FDI_p12", 2: "FDI_p1", 3: "FDI_p32", 4: "FDI_p2", 5: "FDI_p52",
+             6: "FDI_p3", 7: "FDI_p72", 8: "FDI_p4", 9: "FDI_p92", 10: "FDI_p5",
+             11: "FDI_p112", 12: "FDI_p6", 13: "FDI_p132", 14: "FDI_p7", 15: "FDI_p152",
+             16: "FDI_p8", 17: "FDI_p172", 18: "FDI_p9", 19: "FDI_p192", 20: "FDI_p10",
+             21: "FDI_p212"}
+
+
+def _twice_order(order):
+    k2 = int(round(2 * float(order)))
+    if k2 != 2 * float(order) or k2 not in FDI_NAMES:
+        raise ValueError("order must be one of -9/2, -7/2, ..., -1/2, 0, 1/2, 1, ..., 21/2")
+    return k2
+
+
+def fdi(order, x, out=None, stream=None):
+    """Fermi-Dirac integral F_order(x) of a float64 CUDA tensor, unnormalised as
+    the reference's FDI_* functions (order = -9/2 .. -1/2 or 0 .. 21/2 in
+    halves)."""
+    import torch
+    k2 = _twice_order(order)
+    if x.dtype != torch.float64 or not x.is_cuda:
+        raise ValueError("x must be a float64 CUDA tensor")
+    x = x.contiguous()
+    if out is None:
+        out = torch.empty_like(x)
+    _check(C.load().bnsn_fdi(k2, x.data_ptr(), out.data_ptr(), x.numel(),
+                             _stream_handle(stream)))
+    return out
+
+
+def fdi_host(order, x):
+    """F_order(x) of a host float64 array (copied to the GPU and back)."""
+    k2 = _twice_order(order)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty_like(x)
+    _check(C.load().bnsn_fdi_host(k2, x.ctypes.data, out.ctypes.data, x.size))
+    return out
+
+
 def set_gp19_table(tab):
     """Load a GP19 table dict (dims, nb, ye, t, w, [lognb, logw], data)."""
     dims = (ctypes.c_int * 4)(*tab["dims"])

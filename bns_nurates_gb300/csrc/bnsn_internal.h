@@ -135,6 +135,10 @@ struct EquilLaunch
 };
 
 cudaError_t launch_distr_from_m1(const DistrLaunch& L, cudaStream_t stream, int num_sms);
+// Fermi-Dirac integral F_{k2/2} of n arguments (device arrays).
+bool fdi_order_valid(int k2);
+cudaError_t launch_fdi(int k2, const double* x, double* out, int64_t n, cudaStream_t stream,
+                       int num_sms);
 cudaError_t launch_nu_equilibrium(const EquilLaunch& L, cudaStream_t stream, int num_sms);
 
 } // namespace bnsn

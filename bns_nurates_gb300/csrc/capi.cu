@@ -854,6 +854,57 @@ extern "C" int bnsn_compute_m1_opacities_point(const MyQuadrature* quad_1d,
     return BNSN_OK;
 }
 
+extern "C" int bnsn_fdi(int twice_order, const double* x, double* out, int64_t n, void* stream)
+{
+    g_err.clear();
+    if (!fdi_order_valid(twice_order))
+        return fail(BNSN_ERR_ARG, "twice_order must be -9, -7, -5, -3, -1 or 0..21");
+    if (n < 0 || (n > 0 && (!x || !out)))
+        return fail(BNSN_ERR_ARG, "invalid argument");
+    DeviceState* st;
+    int rc = device_state(&st);
+    if (rc)
+        return rc;
+    cudaError_t e = launch_fdi(twice_order, x, out, n, (cudaStream_t)stream, st->num_sms);
+    return e == cudaSuccess ? BNSN_OK : cuda_fail(e, "fdi kernel launch");
+}
+
+extern "C" int bnsn_fdi_host(int twice_order, const double* x, double* out, int64_t n)
+{
+    g_err.clear();
+    if (!fdi_order_valid(twice_order))
+        return fail(BNSN_ERR_ARG, "twice_order must be -9, -7, -5, -3, -1 or 0..21");
+    if (n < 0 || (n > 0 && (!x || !out)))
+        return fail(BNSN_ERR_ARG, "invalid argument");
+    if (n == 0)
+        return BNSN_OK;
+    DeviceState* st;
+    int rc = device_state(&st);
+    if (rc)
+        return rc;
+    const int64_t chunk = std::min<int64_t>(n, (int64_t)1 << 22);
+    std::lock_guard<std::mutex> lk(g_stage_mu);
+    double* buf;
+    if ((rc = stage(st, sizeof(double) * 2 * chunk, &buf)))
+        return rc;
+    cudaStream_t s0 = st->streams[0];
+    for (int64_t p0 = 0; p0 < n; p0 += chunk)
+    {
+        const int64_t m = std::min<int64_t>(chunk, n - p0);
+        cudaError_t err = cudaMemcpyAsync(buf, x + p0, sizeof(double) * m,
+                                          cudaMemcpyHostToDevice, s0);
+        if (err == cudaSuccess)
+            err = launch_fdi(twice_order, buf, buf + chunk, m, s0, st->num_sms);
+        if (err == cudaSuccess)
+            err = cudaMemcpyAsync(out + p0, buf + chunk, sizeof(double) * m,
+                                  cudaMemcpyDeviceToHost, s0);
+        if (err != cudaSuccess)
+            return cuda_fail(err, "fdi host batch");
+    }
+    cudaError_t err = cudaStreamSynchronize(s0);
+    return err == cudaSuccess ? BNSN_OK : cuda_fail(err, "fdi host batch");
+}
+
 extern "C" int bnsn_distr_from_m1_point(const M1Quantities* m1, NuDistributionParams* out)
 {
     g_err.clear();

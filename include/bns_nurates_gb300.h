@@ -432,6 +432,19 @@ int bnsn_m1_opacities_host(const MyQuadrature* quad_1d,
                            const bnsn_m1_soa* m1, int stim_abs, int precision,
                            const bnsn_m1_opacities_soa* out, int64_t npts);
 
+/* Fermi-Dirac integrals F_j(x) = int_0^inf t^j / (exp(t - x) + 1) dt of the
+ * reference's family (functions.hpp:442-4375), unnormalised as there, for
+ * j = twice_order / 2: twice_order -9, -7, -5, -3, -1 replaces FDI_m92 ..
+ * FDI_m12 (continued below j = -1 by dF_{j+1}/dx = (j+1) F_j), 0 .. 21
+ * replaces FDI_0, FDI_p12, FDI_p1, ..., FDI_p10, FDI_p212.  Integer orders 0..5
+ * use the reference's approximations; the others tabulated approximations
+ * that agree with the reference's to a few 1e-16 relative.  A NaN argument
+ * gives NaN (half-integer orders) or 0 (integer orders), as the reference.
+ * bnsn_fdi: x and out are device arrays of n doubles, stream-ordered.
+ * bnsn_fdi_host: host arrays, synchronous.  BNSN_ERR_ARG for another order. */
+int bnsn_fdi(int twice_order, const double* x, double* out, int64_t n, void* stream);
+int bnsn_fdi_host(int twice_order, const double* x, double* out, int64_t n);
+
 /* Gauss-Legendre nodes/weights of order quad->nx on [0,1]; replaces
  * GaussLegendre (integration.hpp:28-87), same algorithm. */
 int bnsn_gauss_legendre(MyQuadrature* quad);

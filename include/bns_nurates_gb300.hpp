@@ -11,6 +11,8 @@
  *       (m1_opacities.hpp:1506-1660)
  *   CalculateDistrParamsFromM1 (distribution.hpp:323-333)
  *   GaussLegendre (integration.hpp:28-87)
+ *   FDI_m92 .. FDI_m12, FDI_0, FDI_p12, FDI_p1, ..., FDI_p10, FDI_p212
+ *       (functions.hpp:442-4375; one argument per call, NaN on error)
  *
  * The reference's functions return no status.  These return the same
  * structs; when the library reports an error (no sm_103 device, an argument
@@ -96,5 +98,42 @@ inline void GaussLegendre(MyQuadrature* quad)
 {
     bnsn_gauss_legendre(quad);
 }
+
+#define BNSN_DROPIN_FDI(NAME, K2)                                                        \
+    inline double NAME(const double x)                                                   \
+    {                                                                                    \
+        double v;                                                                        \
+        return bnsn_fdi_host(K2, &x, &v, 1) == BNSN_OK                                   \
+                   ? v                                                                   \
+                   : std::numeric_limits<double>::quiet_NaN();                           \
+    }
+BNSN_DROPIN_FDI(FDI_m92, -9)
+BNSN_DROPIN_FDI(FDI_m72, -7)
+BNSN_DROPIN_FDI(FDI_m52, -5)
+BNSN_DROPIN_FDI(FDI_m32, -3)
+BNSN_DROPIN_FDI(FDI_m12, -1)
+BNSN_DROPIN_FDI(FDI_0, 0)
+BNSN_DROPIN_FDI(FDI_p12, 1)
+BNSN_DROPIN_FDI(FDI_p1, 2)
+BNSN_DROPIN_FDI(FDI_p32, 3)
+BNSN_DROPIN_FDI(FDI_p2, 4)
+BNSN_DROPIN_FDI(FDI_p52, 5)
+BNSN_DROPIN_FDI(FDI_p3, 6)
+BNSN_DROPIN_FDI(FDI_p72, 7)
+BNSN_DROPIN_FDI(FDI_p4, 8)
+BNSN_DROPIN_FDI(FDI_p92, 9)
+BNSN_DROPIN_FDI(FDI_p5, 10)
+BNSN_DROPIN_FDI(FDI_p112, 11)
+BNSN_DROPIN_FDI(FDI_p6, 12)
+BNSN_DROPIN_FDI(FDI_p132, 13)
+BNSN_DROPIN_FDI(FDI_p7, 14)
+BNSN_DROPIN_FDI(FDI_p152, 15)
+BNSN_DROPIN_FDI(FDI_p8, 16)
+BNSN_DROPIN_FDI(FDI_p172, 17)
+BNSN_DROPIN_FDI(FDI_p9, 18)
+BNSN_DROPIN_FDI(FDI_p192, 19)
+BNSN_DROPIN_FDI(FDI_p10, 20)
+BNSN_DROPIN_FDI(FDI_p212, 21)
+#undef BNSN_DROPIN_FDI
 
 #endif /* BNS_NURATES_GB300_HPP */

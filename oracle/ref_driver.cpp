@@ -268,6 +268,48 @@ void ref_fdi(int k, int64_t n, const double* x, double* out)
     }
 }
 
+// The whole family of functions.hpp:442-4375 by twice the order,
+// k2 = -9, -7, ..., -1 (FDI_m92 .. FDI_m12) and 0..21 (FDI_0, FDI_p12, FDI_p1,
+// ..., FDI_p10, FDI_p212).  Returns -1 for an order the reference lacks.
+int ref_fdi_family(int k2, int64_t n, const double* x, double* out)
+{
+    double (*f)(double) = nullptr;
+    switch (k2)
+    {
+    case -9: f = FDI_m92; break;
+    case -7: f = FDI_m72; break;
+    case -5: f = FDI_m52; break;
+    case -3: f = FDI_m32; break;
+    case -1: f = FDI_m12; break;
+    case 0: f = FDI_0; break;
+    case 1: f = FDI_p12; break;
+    case 2: f = FDI_p1; break;
+    case 3: f = FDI_p32; break;
+    case 4: f = FDI_p2; break;
+    case 5: f = FDI_p52; break;
+    case 6: f = FDI_p3; break;
+    case 7: f = FDI_p72; break;
+    case 8: f = FDI_p4; break;
+    case 9: f = FDI_p92; break;
+    case 10: f = FDI_p5; break;
+    case 11: f = FDI_p112; break;
+    case 12: f = FDI_p6; break;
+    case 13: f = FDI_p132; break;
+    case 14: f = FDI_p7; break;
+    case 15: f = FDI_p152; break;
+    case 16: f = FDI_p8; break;
+    case 17: f = FDI_p172; break;
+    case 18: f = FDI_p9; break;
+    case 19: f = FDI_p192; break;
+    case 20: f = FDI_p10; break;
+    case 21: f = FDI_p212; break;
+    default: return -1;
+    }
+    for (int64_t i = 0; i < n; ++i)
+        out[i] = f(x[i]);
+    return 0;
+}
+
 // Pair kernel at (omega, omega_prime) for one EOS state: out[8] = em[4], abs[4]
 void ref_pair_kernel(double temp, double mu_e, double omega, double omega_prime,
                      double* out)

@@ -3,6 +3,8 @@
 // CalculateDistrParamsFromM1, GaussLegendre) through bns_nurates_gb300.hpp.
 // Prints, for each synthetic point, the 28 distribution parameters, the 20
 // grey outputs and the 16 spectral outputs at 10 MeV, one value per line.
+// With a second argument "fdi": FDI_m92, FDI_m32, FDI_0, FDI_p12, FDI_p3,
+// FDI_p10 and FDI_p212 at -3.5, 0.25, 7 and 60, one value per line.
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -11,6 +13,15 @@
 
 int main(int argc, char** argv)
 {
+    if (argc > 2 && argv[2][0] == 'f')
+    {
+        double (*fn[7])(double) = {FDI_m92, FDI_m32, FDI_0, FDI_p12, FDI_p3, FDI_p10, FDI_p212};
+        const double xs[4]      = {-3.5, 0.25, 7., 60.};
+        for (int f = 0; f < 7; ++f)
+            for (int i = 0; i < 4; ++i)
+                printf("%.17g\n", fn[f](xs[i]));
+        return bnsn_last_error()[0] == 0 ? 0 : 1;
+    }
     const int npts = argc > 1 ? atoi(argv[1]) : 4;
     std::vector<double> eos(11 * npts), m1(12 * npts);
     if (bnsn_synthetic_points(20261203, 0, npts, eos.data(), m1.data(), 1) != BNSN_OK)

@@ -46,3 +46,13 @@ def test_dropin_matches_batched_api(cuda, tmp_path):
     assert np.array_equal(vals[:, :28], distr.cpu().numpy().T)
     assert np.array_equal(vals[:, 28:48], grey.cpu().numpy().T)
     assert np.array_equal(vals[:, 48:], spec.cpu().numpy()[:, :, 0].T)
+
+
+@pytest.mark.gpu
+def test_dropin_fdi_matches_batched_api(cuda, tmp_path):
+    exe = build_program(tmp_path)
+    txt = subprocess.run([exe, "1", "fdi"], check=True, capture_output=True, text=True).stdout
+    vals = np.array([float(v) for v in txt.split()]).reshape(7, 4)
+    xs = np.array([-3.5, 0.25, 7.0, 60.0])
+    for row, order in zip(vals, (-4.5, -1.5, 0, 0.5, 3, 10, 10.5)):
+        assert np.array_equal(row, bn.fdi_host(order, xs)), order
