@@ -1,17 +1,19 @@
 // Grey M1 opacity kernels (sm_103a), FP64 and mixed precision.
 //
 // Restates ComputeM1OpacitiesGenericFormalism (m1_opacities.hpp:1062-1295)
-// with the integration rules of integration.hpp:608-844, as five phase
+// with the integration rules of integration.hpp:608-844, as six phase
 // kernels over a chunk of points.  Each phase has a small hot loop shared by
 // all resident warps, so the instruction working set stays in the SM's
 // instruction cache (a single fused kernel spent most of its issue slots
 // waiting on instruction fetch):
 //
-//   prelude : per point (one warp): distribution parameters, Fermi integrals
-//             at +-eta_e, brem channel constants, the 2n-energy tables of the
-//             double integral (distribution values, F_k(eta +- w/T)), and the
-//             1-D beta and iso-scattering integrals; the per-point record is
-//             staged in shared memory and written to the scratch arena.
+//   point   : per (point, task) (one thread): distribution parameters,
+//             Fermi integrals at +-eta_e, brem and iso constants, written to
+//             the header of the point's scratch record.
+//   prelude : per point (one warp): the 2n-energy tables of the double
+//             integral (distribution values, F_k(eta +- w/T)) and the 1-D beta
+//             and iso-scattering integrals; the per-point record is staged in
+//             shared memory and written to the scratch arena.
 //   pair    : per point (one warp): the M(M+1)/2 unordered (w, w') cells of
 //             the pair kernel, one evaluation filling (w, w') and (w', w),
 //             weighted and summed into the number and energy moments.
@@ -32,6 +34,8 @@
 // distribution-weighted sums stay FP64.
 
 #include <cuda_runtime.h>
+
+#include <cstddef>
 
 #include "bnsn_df.cuh"
 #include "bnsn_fp32.cuh"
@@ -120,6 +124,78 @@ __device__ __forceinline__ void beta_scales(double T, double eta_e, const double
 }
 
 // ---------------------------------------------------------------------------
+// point constants: the per-point quantities that do not depend on an energy
+// node, as 12 independent tasks, one thread per (point, task) with the task
+// in blockIdx.y (every warp runs one code path):
+//   0..3  distribution parameters of species 0..3 (or a copy of the given ones)
+//   4, 5  F_0..F_5 and FermiDistr(0, 1, .) at +eta_e, -eta_e
+//   6..8  HR98 channel constants; 9: HR98 point constants; 10: BRT06 prefactor
+//   11    eta_NN of protons and neutrons (iso scattering)
+// written straight into the point's scratch record, whose header the prelude
+// then loads.  Inside the one-warp-per-point prelude these tasks ran on one to
+// four lanes each, one after the other.
+// ---------------------------------------------------------------------------
+constexpr int kPointTasks = 12;
+
+__global__ void __launch_bounds__(128)
+    grey_point_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
+                      double* __restrict__ scratch)
+{
+    const int task = blockIdx.y;
+    if ((task >= 6 && task <= 9 && !(L.use_brem && L.brem_impl == 0)) ||
+        (task == 10 && !(L.use_brem && L.brem_impl == 1)) || (task == 11 && !L.use_iso))
+        return;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < np;
+         q += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int64_t p = L.pidx ? L.pidx[p0 + q] : p0 + q;
+        PointTab* P     = (PointTab*)(scratch + q * kTabWords);
+        const double nb = L.eos[0][p], T = L.eos[1][p];
+        if (task < 4)
+        {
+            const int s = task;
+            Distr& d    = P->d;
+            if (L.has_distr)
+            {
+#pragma unroll
+                for (int f = 0; f < 7; ++f)
+                    (&d.w_t[0])[f * 4 + s] = L.distr[f * 4 + s][p];
+            }
+            else
+                distr_species(L.m1[s][p], L.m1[4 + s][p], L.m1[8 + s][p], L.gamma36, &d.w_t[s],
+                              &d.temp_t[s], &d.eta_t[s], &d.w_f[s], &d.temp_f[s], &d.c_f[s],
+                              &d.beta_f[s]);
+        }
+        else if (task < 6)
+        {
+            const int e     = task - 4;
+            const double et = e ? -L.eos[7][p] / T : L.eos[7][p] / T;
+            double f[6];
+            fdi_orders<0, 5>(et, f);
+#pragma unroll
+            for (int kk = 0; kk < 6; ++kk)
+                P->fe[e][kk] = f[kk];
+            P->fd0[e] = fermi_distr(0., 1., et);
+        }
+        else if (task < 9)
+            P->hr.ch[task - 6] = hr98_channel(nb, L.eos[4][p], L.eos[3][p], T, task - 6);
+        else if (task == 9)
+            hr98_point_common(nb, T, L.use_medium != 0, &P->hr); // leaves hr.ch alone
+        else if (task == 10)
+            P->brt06_pre = brt06_point(nb, T, L.eos[4][p], L.eos[3][p]);
+        else
+        {
+            P->eta_pp = eta_nn_sc(nb, T, L.eos[3][p]);
+            P->eta_nn = eta_nn_sc(nb, T, L.eos[4][p]);
+        }
+    }
+}
+
+// Words of the record header written by grey_point_kernel (everything
+// before the energy tables).
+constexpr int kHeadWords = (int)(offsetof(PointTab, nu) / sizeof(double));
+
+// ---------------------------------------------------------------------------
 // prelude
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kWarps * 32)
@@ -149,39 +225,10 @@ __global__ void __launch_bounds__(kWarps * 32)
         const double mu_e = L.eos[7][p];
         const double eta_e = mu_e / T;
 
-        if (L.has_distr)
-        {
-            if (lane < 28)
-                (&W.d.w_t[0])[lane] = L.distr[lane][p];
-        }
-        else if (lane < 4)
-        {
-            const int s = lane;
-            distr_species(L.m1[s][p], L.m1[4 + s][p], L.m1[8 + s][p], L.gamma36, &W.d.w_t[s],
-                          &W.d.temp_t[s], &W.d.eta_t[s], &W.d.w_f[s], &W.d.temp_f[s],
-                          &W.d.c_f[s], &W.d.beta_f[s]);
-        }
-        if (lane == 4 || lane == 5)
-        {
-            const int e     = lane - 4;
-            const double et = e ? -mu_e / T : eta_e;
-            fdi_orders<0, 5>(et, W.fe[e]);
-            W.fd0[e] = fermi_distr(0., 1., et);
-        }
-        if (L.use_brem && L.brem_impl == 0)
-        {
-            if (lane >= 6 && lane < 9)
-                W.hr.ch[lane - 6] = hr98_channel(nb, yn, yp, T, lane - 6);
-            if (lane == 9)
-                hr98_point_common(nb, T, L.use_medium != 0, &W.hr);
-        }
-        if (lane == 10 && L.use_brem && L.brem_impl == 1)
-            W.brt06_pre = brt06_point(nb, T, yn, yp);
-        if (lane == 11 && L.use_iso)
-        {
-            W.eta_pp = eta_nn_sc(nb, T, yp);
-            W.eta_nn = eta_nn_sc(nb, T, yn);
-        }
+        // header of the record (distribution, F_k(+-eta_e), brem and iso
+        // constants) from grey_point_kernel
+        __syncwarp();
+        warp_copy((double*)&W, scratch + q * kTabWords, kHeadWords, lane);
         __syncwarp();
         if (lane == 0)
         {
@@ -991,6 +1038,7 @@ __device__ __forceinline__ void neps_item_mixed(const NepsPoint& P, const NepsMi
     const df S  = add(W, WP);
     const df Pp = mul(W, WP);
     const df Dn = mul(Pp, Pp);
+    const df iDn = div(mk(1.f), Dn); // the four brackets per lepton share 1 / Dn
     const df X  = from_double(x), Y = from_double(y);
     // e+ terms scale as e^{-eta_e}: below 1e-13 of the e- terms for eta_e > 30
     const int nlep = P.eta0 > 30. ? 1 : 2;
@@ -1027,10 +1075,10 @@ __device__ __forceinline__ void neps_item_mixed(const NepsPoint& P, const NepsMi
             const df c1 = sub(mul(d2, sign1), w4);
             const df c2 = add(mul(d2, sign2), w4);
             const df s6 = mul(dw[0], 6.f);
-            const df A1 = sub(div(add(sub(c1, ST), mul(U, sign1)), Dn), s6);
-            const df B1 = div(add(c1, mul(V, sign1)), Dn);
-            const df A2 = add(div(add(add(c2, ST), mul(U, sign2)), Dn), s6);
-            const df B2 = div(add(c2, mul(V, sign2)), Dn);
+            const df A1 = sub(mul(add(sub(c1, ST), mul(U, sign1)), iDn), s6);
+            const df B1 = mul(add(c1, mul(V, sign1)), iDn);
+            const df A2 = add(mul(add(add(c2, ST), mul(U, sign2)), iDn), s6);
+            const df B2 = mul(add(c2, mul(V, sign2)), iDn);
             // couplings of neps_couplings: species s pairs (b1, b2) from
             // {B+ or B-, B0} in an order set by the lepton
             constexpr dfc kBp(k::NepsBPlus), kBm(k::NepsBMinus), kBz(k::NepsBZero);
@@ -1122,6 +1170,7 @@ __device__ __forceinline__ void neps_item_df(const NepsPoint& P, const NepsMixed
     const df S  = add(W, WP);
     const df Pp = mul(W, WP);
     const df Dn = mul(Pp, Pp);
+    const df iDn = div(mk(1.f), Dn); // the four brackets per lepton share 1 / Dn
     const df X  = from_double(x), Y = from_double(y);
     // e+ terms scale as e^{-eta_e}: below 1e-13 of the e- terms for eta_e > 30
     const int nlep = P.eta0 > 30. ? 1 : 2;
@@ -1153,10 +1202,10 @@ __device__ __forceinline__ void neps_item_df(const NepsPoint& P, const NepsMixed
             const df c1 = sub(mul(dd2, sign1), dw4);
             const df c2 = add(mul(dd2, sign2), dw4);
             const df s6 = mul(dw[0], 6.f);
-            const df A1 = sub(div(add(sub(c1, ST), mul(U, sign1)), Dn), s6);
-            const df B1 = div(add(c1, mul(V, sign1)), Dn);
-            const df A2 = add(div(add(add(c2, ST), mul(U, sign2)), Dn), s6);
-            const df B2 = div(add(c2, mul(V, sign2)), Dn);
+            const df A1 = sub(mul(add(sub(c1, ST), mul(U, sign1)), iDn), s6);
+            const df B1 = mul(add(c1, mul(V, sign1)), iDn);
+            const df A2 = add(mul(add(add(c2, ST), mul(U, sign2)), iDn), s6);
+            const df B2 = mul(add(c2, mul(V, sign2)), iDn);
             constexpr dfc kBp(k::NepsBPlus), kBm(k::NepsBMinus), kBz(k::NepsBZero);
 #pragma unroll
             for (int s = 0; s < 4; ++s)
@@ -1634,6 +1683,13 @@ cudaError_t launch_grey_chunks(const OpacityLaunch& L, cudaStream_t st0, cudaStr
         double* const wsk     = odd ? ws1 : ws0;
         const int64_t np      = (L.npts - p0) < chunk ? (L.npts - p0) : chunk;
         const int64_t wb      = (np + kWarps - 1) / kWarps;
+        phase_mark(kPhPrelude, 0, st);
+        {
+            const int64_t bx = (np + 127) / 128;
+            const dim3 pgrid((unsigned)(bx < (int64_t)sms * 4 ? bx : (int64_t)sms * 4), kPointTasks);
+            grey_point_kernel<<<pgrid, 128, 0, st>>>(L, p0, np, wsk);
+        }
+        phase_mark(kPhPrelude, 1, st);
         phase_mark(kPhPrelude, 0, st);
         grey_prelude_kernel<<<grid_for(grey_prelude_kernel, kWarps * 32, wb, sms), kWarps * 32, 0,
                               st>>>(L, p0, np, wsk);
