@@ -185,3 +185,20 @@ def test_mixed_spectral_close_to_fp64_gpu(cuda):
     r = rel_err(a, c, floor=1e-300)
     assert np.percentile(r, 99.9) < MIXED_TOL
     assert (np.isfinite(a) == np.isfinite(c)).all()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_spectral_two_stream_chunks_match_single_chunk_calls(cuda, precision):
+    """A batch of three spectral chunks (two streams, two scratch areas) gives
+    bitwise the results of calls on slices that fit one chunk."""
+    n, nsl = 12000, 4000
+    eos, m1 = bn.synthetic_points(11, n, first=5 * 10 ** 6)
+    energies = np.logspace(0., np.log10(300.), 24)
+    fl, pr, q = bn.opacity_flags(), _params((1, 0, 1, 1, 1, 2, 1, 0)), bn.gauss_legendre(20)
+    e = cuda.from_numpy(eos).cuda()
+    m = cuda.from_numpy(m1).cuda()
+    whole = bn.spectral_opacities(e, m, fl, pr, q, energies, precision=precision).cpu().numpy()
+    parts = [bn.spectral_opacities(e[:, k:k + nsl].contiguous(), m[:, k:k + nsl].contiguous(),
+                                   fl, pr, q, energies, precision=precision).cpu().numpy()
+             for k in range(0, n, nsl)]
+    assert np.array_equal(whole, np.concatenate(parts, axis=1), equal_nan=True)
