@@ -107,12 +107,15 @@ cudaError_t launch_grey_chunks(const OpacityLaunch& L, cudaStream_t stream0, cud
 // Spectral opacities (phase kernels over chunks of points).  The scratch of
 // one call holds spectral_scratch_bytes(chunk, n_energies) bytes for chunks of
 // spectral_chunk_points(n_energies) points (about kSpecChunkRecords
-// (point, energy) records of 256 bytes).
+// (point, energy) records of 256 bytes).  With aux and scratch1 (a second
+// scratch of the same size) consecutive chunks alternate between stream and
+// aux; stream waits for aux at the end.
 constexpr int64_t kSpecChunkRecords = 131072;
 int64_t spectral_chunk_points(int n_energies);
 size_t spectral_scratch_bytes(int64_t chunk_points, int n_energies);
 cudaError_t launch_spectral(const OpacityLaunch& L, cudaStream_t stream, int num_sms,
-                            void* scratch, int64_t chunk_points);
+                            void* scratch, int64_t chunk_points, cudaStream_t aux = nullptr,
+                            void* scratch1 = nullptr);
 cudaError_t spectral_mixed_counts(unsigned long long* counts, bool reset);
 // Outputs holding a NaN or Inf since the last reset: grey points, spectral
 // (point, energy) pairs (synchronous reads of the current device's counters).

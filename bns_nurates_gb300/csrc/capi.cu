@@ -579,18 +579,24 @@ int bnsn_spectral_opacities(const MyQuadrature* quad_1d, const OpacityFlags* fla
         return BNSN_OK;
     const int ne_max     = n_energies < 64 ? n_energies : 64;
     const int64_t chunk  = std::min<int64_t>(npts, spectral_chunk_points(ne_max));
+    // more than one chunk: a second scratch, chunks alternating with the aux stream
+    const bool two       = npts > chunk && st->aux != nullptr;
+    const size_t wbytes  = spectral_scratch_bytes(chunk, ne_max);
+    const size_t wpad    = (wbytes + 255) & ~(size_t)255;
     void* ws             = nullptr;
-    cudaError_t e = cudaMallocFromPoolAsync(&ws, spectral_scratch_bytes(chunk, ne_max), st->pool,
+    cudaError_t e = cudaMallocFromPoolAsync(&ws, two ? wpad + wbytes : wbytes, st->pool,
                                             (cudaStream_t)stream);
     if (e != cudaSuccess)
         return cuda_fail(e, "spectral scratch allocation");
+    void* ws1 = two ? (void*)((char*)ws + wpad) : nullptr;
     for (int e0 = 0; e0 < n_energies && e == cudaSuccess; e0 += 64)
     {
         L.n_energies = (n_energies - e0) < 64 ? (n_energies - e0) : 64;
         L.e_offset   = e0;
         for (int k = 0; k < L.n_energies; ++k)
             L.energies[k] = energies[e0 + k];
-        e = launch_spectral(L, (cudaStream_t)stream, st->num_sms, ws, chunk);
+        e = launch_spectral(L, (cudaStream_t)stream, st->num_sms, ws, chunk,
+                            two ? st->aux : nullptr, ws1);
     }
     const cudaError_t ef = cudaFreeAsync(ws, (cudaStream_t)stream);
     if (e != cudaSuccess)

@@ -1112,22 +1112,46 @@ cudaError_t spectral_nonfinite_count(unsigned long long* count, bool reset)
     return e;
 }
 
-cudaError_t launch_spectral(const OpacityLaunch& L, cudaStream_t st, int sms, void* scratch,
-                            int64_t chunk_points)
+cudaError_t launch_spectral(const OpacityLaunch& L, cudaStream_t st0, int sms, void* scratch,
+                            int64_t chunk_points, cudaStream_t aux, void* scratch1)
 {
     if (L.npts <= 0 || L.n_energies <= 0)
         return cudaSuccess;
     const int ne     = L.n_energies;
     const int G      = pick_groups(ne < kEChunk ? ne : kEChunk, 2 * L.n1);
-    double* dsc      = (double*)scratch;
-    uint64_t* fl_pb  = (uint64_t*)(dsc + chunk_points * 28);
-    uint64_t* fl_nes = fl_pb + chunk_points;
-    EnergyRec* rec   = (EnergyRec*)(fl_nes + chunk_points);
     const bool pb    = L.use_pair || L.use_brem;
     const bool inel  = L.use_inel != 0;
-    cudaError_t err  = cudaSuccess;
-    for (int64_t p0 = 0; p0 < L.npts && err == cudaSuccess; p0 += chunk_points)
+    // With an auxiliary stream and scratch, consecutive chunks alternate
+    // between the caller's stream and aux: the redo passes of one chunk (few
+    // flagged records, a mostly idle grid) run beside the main passes of the
+    // other.  The caller's stream waits for aux at the end.
+    const bool two    = aux != nullptr && scratch1 != nullptr && L.npts > chunk_points;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    if (two)
     {
+        cudaError_t e;
+        if ((e = cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaEventRecord(ev[0], st0)) != cudaSuccess ||
+            (e = cudaStreamWaitEvent(aux, ev[0], 0)) != cudaSuccess)
+        {
+            if (ev[0])
+                cudaEventDestroy(ev[0]);
+            if (ev[1])
+                cudaEventDestroy(ev[1]);
+            return e;
+        }
+    }
+    cudaError_t err = cudaSuccess;
+    int64_t k       = 0;
+    for (int64_t p0 = 0; p0 < L.npts && err == cudaSuccess; p0 += chunk_points, ++k)
+    {
+        const bool odd        = two && (k & 1);
+        const cudaStream_t st = odd ? aux : st0;
+        double* dsc           = (double*)(odd ? scratch1 : scratch);
+        uint64_t* fl_pb       = (uint64_t*)(dsc + chunk_points * 28);
+        uint64_t* fl_nes      = fl_pb + chunk_points;
+        EnergyRec* rec        = (EnergyRec*)(fl_nes + chunk_points);
         const int64_t np  = (L.npts - p0) < chunk_points ? (L.npts - p0) : chunk_points;
         const int64_t nth = np * 4;
         phase_mark(kPhSpectral, 0, st);
@@ -1164,6 +1188,15 @@ cudaError_t launch_spectral(const OpacityLaunch& L, cudaStream_t st, int sms, vo
                       ? launch_assemble<kSpecRedo>(L, p0, np, dsc, rec, fl_pb, fl_nes, st, sms)
                       : launch_assemble<kSpecFinal>(L, p0, np, dsc, rec, fl_pb, fl_nes, st, sms);
         }
+    }
+    if (two)
+    {
+        const cudaError_t e1 = cudaEventRecord(ev[1], aux);
+        const cudaError_t e2 = e1 == cudaSuccess ? cudaStreamWaitEvent(st0, ev[1], 0) : e1;
+        cudaEventDestroy(ev[0]);
+        cudaEventDestroy(ev[1]);
+        if (err == cudaSuccess)
+            err = e2;
     }
     return err;
 }
