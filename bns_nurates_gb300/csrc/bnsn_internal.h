@@ -75,7 +75,7 @@ void phase_mark(int phase, int end, cudaStream_t stream);
 // scratch records of grey_point_scratch_bytes() (= kGreyRecordBytes) each.
 // With an auxiliary stream (launch_grey's aux, else nullptr) the chunks are
 // ws_points / 2 points, alternating between the two streams.
-constexpr size_t kGreyRecordBytes = 767 * sizeof(double);
+constexpr size_t kGreyRecordBytes = 800 * sizeof(double);
 size_t grey_point_scratch_bytes();
 
 // C-ABI helpers shared by the entry-point translation units (capi.cu).

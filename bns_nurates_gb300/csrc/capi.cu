@@ -57,7 +57,7 @@ struct DeviceState
     cudaMemPool_t pool = nullptr; // grey scratch records
 };
 
-// Points per grey scratch chunk: 8192 records of ~6 KB (50 MB) stay resident
+// Points per grey scratch chunk: 8192 records of 6.4 KB (52 MB) stay resident
 // in L2 between the phase kernels of a chunk (the batched-blocks autotuner
 // picks this size on most configurations).
 constexpr int64_t kGreyChunk = 8192;

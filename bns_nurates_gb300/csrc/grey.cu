@@ -66,7 +66,10 @@ struct PointTab
     double snes[16];     // NES/NPS, same layout
     double sbeta[8];     // beta: n_em[2], j_em[2], n_ab[2], j_ab[2]
     double siso[4];      // iso per species
+    double sbrem[16];    // brem alone (its part of s2d)
+    double bmag[16];     // mixed path: sum of |term| of FP32 brem cells (s2d units), else 0
     double neps_fp64;    // mixed path: 1 if the NES sums of the point must be FP64
+    double bredo;        // mixed path: 1 if the brem sums must be recomputed in FP64
 };
 static_assert(sizeof(PointTab) % sizeof(double) == 0, "PointTab must be double words");
 static_assert(sizeof(PointTab) == kGreyRecordBytes, "grey record size");
@@ -679,7 +682,7 @@ struct Gp19Warp
 template <bool MIXED, int IMPL>
 __global__ void __launch_bounds__(kWarps * 32)
     grey_brem_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
-                     double* __restrict__ scratch, int add)
+                     double* __restrict__ scratch, int add, int redo_only)
 {
     __shared__ double s_A1[kMaxM], s_A2[kMaxM];
     __shared__ dfm::df s_A1d[MIXED ? kMaxM : 1], s_A2d[MIXED ? kMaxM : 1];
@@ -732,6 +735,8 @@ __global__ void __launch_bounds__(kWarps * 32)
     {
         const int64_t p = L.pidx ? L.pidx[p0 + q] : p0 + q;
         PointTab* P     = (PointTab*)(scratch + q * kTabWords);
+        if (redo_only && P->bredo != 1.)
+            continue; // warp-uniform: one point per warp
         const double T  = L.eos[1][p];
         __syncwarp();
         load_cell_tab(C, P, M, false, lane);
@@ -762,10 +767,10 @@ __global__ void __launch_bounds__(kWarps * 32)
         // (pair + brem + ...) cancel and would magnify FP32 rounding.
         const bool fp32_cells =
             MIXED && (IMPL == 0 || (IMPL == 2 && prof && GW.pt.regime != 3 && GW.pt.regime != 5));
-        double acc[16];
+        double acc[16], bm[16];
 #pragma unroll
         for (int kk = 0; kk < 16; ++kk)
-            acc[kk] = 0.;
+            acc[kk] = bm[kk] = 0.;
         bool redo = false;
         if (fp32_cells)
         {
@@ -873,7 +878,10 @@ __global__ void __launch_bounds__(kWarps * 32)
             redo = cancel_factor(acc, A.mag, scale, scale, other) > kMaxCancelBrem;
 #pragma unroll
             for (int kk = 0; kk < 16; ++kk)
+            {
                 acc[kk] = redo ? 0. : acc[kk] * scale;
+                bm[kk]  = redo ? 0. : warp_sum((double)A.mag[kk]) * scale;
+            }
         }
         if (!fp32_cells || redo)
         {
@@ -924,9 +932,15 @@ __global__ void __launch_bounds__(kWarps * 32)
             acc[kk] = warp_sum(acc[kk]);
         if (lane == 0)
         {
+            // a redo replaces the FP32 brem part of s2d by the FP64 one
 #pragma unroll
             for (int kk = 0; kk < 16; ++kk)
-                P->s2d[kk] = add ? P->s2d[kk] + acc[kk] : acc[kk];
+            {
+                const double base = add ? (redo_only ? P->s2d[kk] - P->sbrem[kk] : P->s2d[kk]) : 0.;
+                P->s2d[kk]   = base + acc[kk];
+                P->sbrem[kk] = acc[kk];
+                P->bmag[kk]  = bm[kk];
+            }
         }
     }
 }
@@ -1532,14 +1546,21 @@ __device__ unsigned long long g_grey_nonfinite;
 
 __global__ void __launch_bounds__(128)
     grey_final_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
-                      const double* __restrict__ scratch)
+                      double* __restrict__ scratch, int redo_only)
 {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < np;
          q += (int64_t)gridDim.x * blockDim.x)
     {
         bool nonfinite      = false;
         const int64_t p     = L.pidx ? L.pidx[p0 + q] : p0 + q;
-        const PointTab* P   = (const PointTab*)(scratch + q * kTabWords);
+        PointTab* P         = (PointTab*)(scratch + q * kTabWords);
+        if (redo_only && P->bredo != 1.)
+            continue;
+        // mixed path: FP32 brem terms whose sum the other reactions cancel
+        // (the NES sums of the opposite sign where the occupation exceeds 1)
+        // by more than kMaxCancelBrem are recomputed in FP64 (bredo = 1)
+        const bool check = !redo_only && L.mixed && L.use_brem;
+        bool bredo       = false;
         const double T      = L.eos[1][p];
         const double eta_e  = L.eos[7][p] / T;
         const double t2d    = k::TempMultiple * T;
@@ -1571,9 +1592,9 @@ __global__ void __launch_bounds__(128)
             const double ene_ab = L.use_inel ? P->snes[12 + s] * hn : 0.;
             const double iso    = L.use_iso ? P->siso[s] * s_iso : 0.;
             double o[5];
+            double bne = 0., bje = 0., bna = 0., bja = 0.;
             if (s < 2)
             {
-                double bne = 0., bje = 0., bna = 0., bja = 0.;
                 if (L.use_abs_em)
                 {
                     bne = P->sbeta[s] * sb[s];
@@ -1598,6 +1619,19 @@ __global__ void __launch_bounds__(128)
                 o[3] = (J > k::ThresholdJ) ? F2 / (c * J) * (e2d_ab + ene_ab) : 0.;
             }
             o[4] = (J > k::ThresholdJ) ? F / (c * J) * iso : 0.;
+            if (check)
+            {
+                // totals of the four moments before the output factors, and the
+                // brem terms' magnitude in the same units
+                const double tot[4] = {F * (n2d_em + nne_em) + bne, F * (n2d_ab + nne_ab) + bna,
+                                       F * (e2d_em + ene_em) + bje, F * (e2d_ab + ene_ab) + bja};
+#pragma unroll
+                for (int m = 0; m < 4; ++m)
+                {
+                    const double mag = F * P->bmag[4 * m + s] * (m < 2 ? t2 : t2d * t2);
+                    bredo = bredo || mag > kMaxCancelBrem * fabs(tot[m]);
+                }
+            }
 #pragma unroll
             for (int qq = 0; qq < 5; ++qq)
             {
@@ -1605,7 +1639,9 @@ __global__ void __launch_bounds__(128)
                 nonfinite = nonfinite || !isfinite(o[qq]);
             }
         }
-        if (nonfinite)
+        if (check)
+            P->bredo = bredo ? 1. : 0.;
+        if (nonfinite && !redo_only)
             atomicAdd(&g_grey_nonfinite, 1ull);
     }
 }
@@ -1629,22 +1665,22 @@ int grid_for(K kernel, int threads, int64_t work, int num_sms)
 
 template <bool MIXED>
 cudaError_t launch_brem(const OpacityLaunch& L, int64_t p0, int64_t np, double* ws,
-                        cudaStream_t st, int sms, int add)
+                        cudaStream_t st, int sms, int add, int redo_only = 0)
 {
     const int64_t wb = (np + kWarps - 1) / kWarps;
     phase_mark(kPhBrem, 0, st);
     if (L.brem_impl == 0)
         grey_brem_kernel<MIXED, 0>
             <<<grid_for(grey_brem_kernel<MIXED, 0>, kWarps * 32, wb, sms), kWarps * 32, 0, st>>>(
-                L, p0, np, ws, add);
+                L, p0, np, ws, add, redo_only);
     else if (L.brem_impl == 1)
         grey_brem_kernel<MIXED, 1>
             <<<grid_for(grey_brem_kernel<MIXED, 1>, kWarps * 32, wb, sms), kWarps * 32, 0, st>>>(
-                L, p0, np, ws, add);
+                L, p0, np, ws, add, redo_only);
     else
         grey_brem_kernel<MIXED, 2>
             <<<grid_for(grey_brem_kernel<MIXED, 2>, kWarps * 32, wb, sms), kWarps * 32, 0, st>>>(
-                L, p0, np, ws, add);
+                L, p0, np, ws, add, redo_only);
     phase_mark(kPhBrem, 1, st);
     return cudaGetLastError();
 }
@@ -1743,8 +1779,18 @@ cudaError_t launch_grey_chunks(const OpacityLaunch& L, cudaStream_t st0, cudaStr
         }
         phase_mark(kPhFinal, 0, st);
         grey_final_kernel<<<grid_for(grey_final_kernel, 128, (np + 127) / 128, sms), 128, 0, st>>>(
-            L, p0, np, wsk);
+            L, p0, np, wsk, 0);
         phase_mark(kPhFinal, 1, st);
+        if (L.mixed && L.use_brem)
+        {
+            // points whose FP32 brem sums the NES sums cancel: brem in FP64, outputs again
+            if ((err = launch_brem<false>(L, p0, np, wsk, st, sms, L.use_pair, 1)) != cudaSuccess)
+                break;
+            phase_mark(kPhFinal, 0, st);
+            grey_final_kernel<<<grid_for(grey_final_kernel, 128, (np + 127) / 128, sms), 128, 0,
+                                st>>>(L, p0, np, wsk, 1);
+            phase_mark(kPhFinal, 1, st);
+        }
         err = cudaGetLastError();
     }
     return err;

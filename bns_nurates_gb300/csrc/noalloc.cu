@@ -1,7 +1,7 @@
 // Static device scratch of bnsn_m1_opacities_noalloc.
 //
 // The array below holds kNoAllocPoints = 4096 grey scratch records of
-// kGreyRecordBytes = 6,136 bytes (24 MiB in all).  It is part of this
+// kGreyRecordBytes = 6,400 bytes (25 MiB in all).  It is part of this
 // translation unit's module, so the CUDA driver places it when the module is
 // loaded; no call of the library allocates or frees it.  Its address is
 // looked up once per device, with that device current, by
