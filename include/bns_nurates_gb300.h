@@ -190,12 +190,16 @@ typedef struct SpectralOpacities
  * stream-ordered on `stream` (a cudaStream_t; NULL = default stream) and do
  * not synchronise the host.
  *
- * Device memory: bnsn_m1_opacities keeps a per-point scratch record (about
- * 6 KB) for at most 8192 points at a time.  It takes that scratch from a
- * library-owned stream-ordered memory pool (one per device, created on the
- * first call), allocating and freeing it in order on `stream`, so calls on
- * different streams never share scratch.  The pool keeps its memory for
- * later calls.  The other batched calls allocate nothing.
+ * Device memory: bnsn_m1_opacities keeps a per-point scratch record (6.4 KB)
+ * for at most 8192 points at a time (two such chunks for larger batches).
+ * It takes that scratch from a library-owned stream-ordered memory pool (one
+ * per device, created on the first call), allocating and freeing it in order
+ * on `stream`, so calls on different streams never share scratch.  The pool
+ * keeps its memory for later calls.  bnsn_spectral_opacities takes its
+ * scratch (256 B per (point, energy) record, about 131,072 records per chunk,
+ * two chunks for larger batches) from the same pool; bnsn_m1_opacities_noalloc
+ * uses a static device array; the host-buffer calls copy through a
+ * library-owned staging buffer.  The other batched calls allocate nothing.
  * ====================================================================== */
 
 typedef enum bnsn_status
