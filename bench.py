@@ -63,6 +63,9 @@ WORKLOADS = {
                     ".005, ~12.9M points), per block: brem HR98/BRT06/GP19, NES on/off, n=10 "
                     "(rho<1e11) or 20; one step = one replay of the CUDA graph of the tuned "
                     "plan over all blocks"),
+    "aux": dict(npts=1 << 24, flags=None, brem=None, nq=None,
+                desc="auxiliary batched kernels on 16,777,216 arguments/points: the Fermi-Dirac "
+                     "family FDI_m92..FDI_p212, CalculateDistrParamsFromM1, NuEquilibriumParams"),
     "c5": dict(npts=256 * 256 * 16, flags=(1, 1, 1, 1, 1), brem=2, nq=20,
                desc="256^3 all reactions (beta+WM+mean field, iso, pair, GP19 brem, NES/NPS), "
                     "n=20; one step = one 256x256x16 slab = 1,048,576 points"),
@@ -199,6 +202,10 @@ def run_reference(args, rank, world):
     libbuild.build()
     wl = dict(WORKLOADS[args.workload])
     nthreads = os.cpu_count()
+    if args.workload == "aux":
+        print(json.dumps({"impl": "reference", "unavailable": "the aux workload times library "
+                          "kernels only; the reference has no batched form of them"}))
+        return
     if args.workload == "c4":
         run_reference_blocks(args, wl, nthreads)
         return
@@ -295,6 +302,69 @@ def timed_steps(step, steps, stream, torch):
     t1.record(stream)
     torch.cuda.synchronize()
     return t0.elapsed_time(t1)
+
+
+def run_aux(args, rank):
+    """Throughput of the auxiliary batched kernels on inputs larger than L2:
+    every order of the Fermi-Dirac family (bnsn_fdi, 8 B in + 8 B out per
+    argument, arguments uniform in [-50, 150] so that every regime is hit),
+    distribution parameters from M1 moments (96 B in, 224 B out per point) and
+    the equilibrium distribution with its M1 densities (32 B in, 320 B out)."""
+    import torch
+    import bns_nurates_gb300 as bn
+    from bns_nurates_gb300 import build as libbuild
+    libbuild.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    n = args.npts or WORKLOADS["aux"]["npts"]
+    stream = torch.cuda.current_stream(dev)
+    warmup = max(args.warmup, 3)
+    gen = torch.Generator(device=dev).manual_seed(SEED)
+    x = torch.rand(n, dtype=torch.float64, device=dev, generator=gen) * 200. - 50.
+    y = torch.empty_like(x)
+    peaks = load_json("MEASURED_PEAKS.json")
+    hbm = peaks.get("hbm_gbs")
+    fp64_peak = bn.fp64_peak_tflops()
+    res = {}
+
+    def timed(fn, nbytes, count):
+        for _ in range(warmup):
+            fn()
+        ms = timed_steps(fn, args.steps, stream, torch) / args.steps
+        gbs = nbytes * count / (ms * 1e-3) / 1e9
+        return {"ms": ms, "per_s": count / (ms * 1e-3), "gbs": gbs,
+                "hbm_frac": gbs / hbm if hbm else None}
+
+    l0 = bn.kernel_launches()
+    fdi = {}
+    for k2 in sorted(bn.FDI_NAMES):
+        r = timed(lambda: bn.fdi(k2 / 2, x, out=y, stream=stream), 16, n)
+        fdi[bn.FDI_NAMES[k2]] = {"args_per_s": r["per_s"], "ms": r["ms"], "gbs": r["gbs"],
+                                 "hbm_frac": r["hbm_frac"]}
+    # one point per workload row: distribution parameters and equilibrium
+    npts = min(n, 1 << 22)
+    eos_h, m1_h = bn.synthetic_points(SEED, npts)
+    eos = torch.from_numpy(eos_h).to(dev)
+    m1 = torch.from_numpy(m1_h).to(dev)
+    d_out = torch.empty((28, npts), dtype=torch.float64, device=dev)
+    res["distr_from_m1"] = timed(lambda: bn.distr_from_m1(m1, out=d_out, stream=stream),
+                                 12 * 8 + 28 * 8, npts)
+    res["nu_equilibrium"] = timed(lambda: bn.nu_equilibrium(eos, stream=stream),
+                                  4 * 8 + 40 * 8, npts)
+    launches = bn.kernel_launches() - l0
+    rates = [v["args_per_s"] for v in fdi.values()]
+    line = {
+        "metric": "auxiliary kernels throughput", "workload": "aux", "unit": "arguments/s",
+        "value": statistics.median(rates), "n_gpus": 1, "steps": args.steps, "warmup": warmup,
+        "higher_is_better": True, "dtype": "f64", "data": "synthetic (uniform arguments; seeded "
+        "generator points)", "config": {"workload": WORKLOADS["aux"]["desc"], "fdi_arguments": n,
+        "points": npts, "l2": "inputs and outputs (256 MB per FDI call) larger than L2"},
+        "fdi": fdi, "distr_from_m1": res["distr_from_m1"], "nu_equilibrium": res["nu_equilibrium"],
+        "peaks": {"hbm_gbs": hbm, "fp64_tflops_probe": fp64_peak},
+        "gpu_launches": launches,
+    }
+    if rank == 0:
+        print(json.dumps(line))
 
 
 C4_EDGES = (8, 16, 24, 32, 48, 64)
@@ -534,6 +604,9 @@ def main():
         return
     if args.workload == "c4":
         run_blocks(args, rank, world, local)
+        return
+    if args.workload == "aux":
+        run_aux(args, rank)
         return
 
     import torch

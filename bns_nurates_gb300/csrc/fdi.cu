@@ -16,8 +16,9 @@
 // half-integer orders and 0 for the integer ones; -inf gives 0; +inf gives
 // +inf for j > -1 and -0 or +0 (the sign of x^(j+1) / (j+1)) below.
 //
-// One thread per argument, grid-stride; FP64-pipe bound (about 60 FP64
-// operations per argument against 16 bytes of traffic).
+// One thread per argument, grid-stride, the order's coefficients staged in
+// shared memory per CTA; FP64-pipe bound (about 60 FP64 operations per
+// argument against 16 bytes of traffic).
 
 #include <cuda_runtime.h>
 
@@ -39,19 +40,50 @@ constexpr int slot_of(int k2)
     return -1;
 }
 
-__device__ __forceinline__ double fdi_table(int slot, double j1, bool integer, double x)
+// One order's coefficients staged in shared memory; the Chebyshev table is
+// transposed to [term][interval] so that the lanes of a warp, which read the
+// same term of different intervals, hit consecutive words.
+struct FdiShared
 {
+    double series[fdit::kSeriesTerms];
+    double cheb[fdit::kChebTerms][fdit::kPieces];
+    double asym[fdit::kAsymTerms];
+};
+
+// x^(h/2) for x >= 100 (or +inf) and |h| <= 23: an integer power by repeated
+// squaring, times sqrt(x) for odd h, inverted for negative h (far cheaper
+// than pow, within a few ulp).
+__device__ __forceinline__ double pow_half(double x, int h)
+{
+    const int a = h < 0 ? -h : h;
+    int q       = a >> 1;
+    double v = 1., b = x;
+    while (q)
+    {
+        if (q & 1)
+            v *= b;
+        q >>= 1;
+        if (q)
+            b *= b;
+    }
+    if (a & 1)
+        v *= sqrt(x);
+    return h < 0 ? 1. / v : v;
+}
+
+__device__ __forceinline__ double fdi_table(const FdiShared& S, int h, bool integer, double x)
+{
+    const double j1 = 0.5 * h; // j + 1
     using namespace fdit;
     if (x < kXlo)
     {
         // sum_n (-1)^(n+1) c_n e^(n x) = e^x sum_m c_(m+1) (-e^x)^m
         const double e = exp(x);
         const double z = -e;
-        const double* c = kSeries[slot];
-        double p = c[kSeriesTerms - 1];
+        double p       = S.series[kSeriesTerms - 1];
 #pragma unroll
         for (int n = kSeriesTerms - 2; n >= 0; --n)
-            p = fma(p, z, c[n]);
+            p = fma(p, z, S.series[n]);
         return e * p;
     }
     if (x < kXhi)
@@ -75,29 +107,27 @@ __device__ __forceinline__ double fdi_table(int slot, double j1, bool integer, d
         }
         const double t  = (x - cen) * sc;
         const double t2 = 2. * t;
-        const double* c = kCheb[slot][i];
         // Clenshaw recurrence for sum_m c_m T_m(t) (c_0 stored halved)
         double b1 = 0., b2 = 0.;
 #pragma unroll
         for (int m = kChebTerms - 1; m >= 1; --m)
         {
-            const double b0 = fma(t2, b1, c[m] - b2);
+            const double b0 = fma(t2, b1, S.cheb[m][i] - b2);
             b2              = b1;
             b1              = b0;
         }
-        return fma(t, b1, c[0] - b2);
+        return fma(t, b1, S.cheb[0][i] - b2);
     }
     if (x != x) // NaN fails both regime tests above
         return integer ? 0. : x;
     // x^(j+1) / (j+1) (1 + sum_k a_k x^(-2k))
-    const double u  = 1. / (x * x);
-    const double* a = kAsym[slot];
-    double s        = a[kAsymTerms - 1];
+    const double u = 1. / (x * x);
+    double s       = S.asym[kAsymTerms - 1];
 #pragma unroll
     for (int k = kAsymTerms - 2; k >= 0; --k)
-        s = fma(s, u, a[k]);
+        s = fma(s, u, S.asym[k]);
     s = fma(s, u, 1.);
-    return pow(x, j1) / j1 * s;
+    return pow_half(x, h) / j1 * s;
 }
 
 template <int K>
@@ -108,12 +138,24 @@ __global__ void fdi_int_kernel(const double* __restrict__ x, double* __restrict_
         out[i] = fdi<K>(x[i]);
 }
 
-__global__ void fdi_table_kernel(int slot, double j1, int integer, const double* __restrict__ x,
+__global__ void fdi_table_kernel(int slot, int h, int integer, const double* __restrict__ x,
                                  double* __restrict__ out, int64_t n)
 {
+    using namespace fdit;
+    __shared__ FdiShared S;
+    for (int k = threadIdx.x; k < kSeriesTerms; k += blockDim.x)
+        S.series[k] = kSeries[slot][k];
+    for (int k = threadIdx.x; k < kPieces * kChebTerms; k += blockDim.x)
+    {
+        const int i = k / kChebTerms, m = k - i * kChebTerms;
+        S.cheb[m][i] = kCheb[slot][i][m];
+    }
+    for (int k = threadIdx.x; k < kAsymTerms; k += blockDim.x)
+        S.asym[k] = kAsym[slot][k];
+    __syncthreads();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
-        out[i] = fdi_table(slot, j1, integer != 0, x[i]);
+        out[i] = fdi_table(S, h, integer != 0, x[i]);
 }
 
 } // namespace
@@ -143,8 +185,7 @@ cudaError_t launch_fdi(int k2, const double* x, double* out, int64_t n, cudaStre
     case 8: fdi_int_kernel<4><<<grid, threads, 0, stream>>>(x, out, n); break;
     case 10: fdi_int_kernel<5><<<grid, threads, 0, stream>>>(x, out, n); break;
     default:
-        fdi_table_kernel<<<grid, threads, 0, stream>>>(slot, 0.5 * k2 + 1., (k2 & 1) == 0, x,
-                                                        out, n);
+        fdi_table_kernel<<<grid, threads, 0, stream>>>(slot, k2 + 2, (k2 & 1) == 0, x, out, n);
     }
     phase_mark(kPhAux, 1, stream);
     return cudaGetLastError();

@@ -21,7 +21,8 @@ FDI_p6 .. FDI_p10) is evaluated in three regimes with tables made here:
   x >= 100      : the Sommerfeld expansion
                   x^{j+1} / (j+1) (1 + sum_k 2 eta(2k) (j+1)(j)...(j+2-2k) x^{-2k}),
                   12 terms; the truncation and the exponentially small
-                  remainder are below 1e-20 of the leading term
+                  remainder are below 1e-20 of the leading term; x^{j+1}
+                  by repeated squaring times sqrt(x) for half-integer j
 
 ``generate()`` computes the coefficients with mpmath at 34 digits and writes
 csrc/bnsn_fdi_tab.h (checked in; mpmath is only needed to regenerate it).
@@ -145,7 +146,7 @@ def generate(path=HEADER, workers=None):
     lines = [
         "// Generated by bns_nurates_gb300/fdi_tables.py (mpmath %s, %d digits); do not edit."
         % (mp.__version__, DPS),
-        "// Tables of the Fermi-Dirac integral family evaluated by bnsn_fdi.cuh:",
+        "// Tables of the Fermi-Dirac integral family evaluated by fdi.cu:",
         "// alternating-series coefficients (x < -4), Chebyshev coefficients of",
         "// the intervals of [-4, 100) and Sommerfeld coefficients (x >= 100).",
         "#pragma once",
@@ -209,6 +210,24 @@ def load_header(path=HEADER):
     }
 
 
+def pow_half(x, h):
+    """x^(h/2) as the kernel forms it: an integer power by repeated squaring,
+    times sqrt(x) for odd h, inverted for negative h."""
+    a = abs(h)
+    q = a >> 1
+    v = np.ones_like(x)
+    b = x.copy()
+    while q:
+        if q & 1:
+            v = v * b
+        q >>= 1
+        if q:
+            b = b * b
+    if a & 1:
+        v = v * np.sqrt(x)
+    return 1.0 / v if h < 0 else v
+
+
 def evaluate(k2, x, tabs):
     """F_{k2/2}(x) for a table order, in FP64 with the kernel's operation order."""
     slot = ORDERS2.index(k2)
@@ -249,7 +268,7 @@ def evaluate(k2, x, tabs):
         for k in range(ASYM_TERMS - 2, -1, -1):
             s = s * u + a[k]
         s = s * u + 1.0
-        out[hi] = np.power(xh, j1) / j1 * s
+        out[hi] = pow_half(xh, k2 + 2) / j1 * s
     nan = np.isnan(x)
     out[nan] = 0.0 if k2 % 2 == 0 else np.nan
     return out
