@@ -34,13 +34,13 @@ struct Group
     int64_t* pidx = nullptr;
     int64_t npts  = 0;
     int64_t chunk = 8192; // points per scratch chunk (untuned default)
-    double grid   = 2.;   // persistent-grid scale (untuned default)
+    double grid   = 4.;   // persistent-grid scale (untuned default)
 };
 
 // Candidate launch shapes of the tuner: (points per chunk, grid scale), timed
 // on at most kTunePoints points of each group.
 const int64_t kChunks[] = {4096, 8192, 16384, 32768};
-const double kGrids[]   = {1., 2.};
+const double kGrids[]   = {2., 4.};
 constexpr int64_t kTunePoints = 65536;
 
 int fill_points_soa(const bnsn_eos_soa* eos, const bnsn_m1_soa* m1,

@@ -1705,12 +1705,13 @@ cudaError_t launch_grey_chunks(const OpacityLaunch& L, cudaStream_t st0, cudaStr
         return cudaSuccess;
     if (!ws0 || (aux && !ws1) || chunk < 1 || !k)
         return cudaErrorInvalidValue;
-    // default grid: two waves of resident CTAs per phase kernel (per-point
-    // work is uneven; the second wave fills the tail of the first, and the
-    // other stream's kernel the tail of both).  Half a wave per stream, so
-    // that both streams' kernels stay resident side by side, measured 15%
-    // slower on the 256^3 all-reactions slab.
-    g_grid_scale = L.grid_scale > 0. ? L.grid_scale : 2.;
+    // default grid: four waves of resident CTAs per phase kernel (per-point
+    // work is uneven; later waves fill the tails of earlier ones, and the
+    // other stream's kernel the tail of both).  Measured on the 256^3
+    // all-reactions slab: 2, 3, 4 waves gave 411k, 417k, 423k points/s mixed
+    // (FP64 172k, 174k, 177k); half a wave per stream, so that both streams'
+    // kernels stay resident side by side, was 15% slower than 2 waves.
+    g_grid_scale = L.grid_scale > 0. ? L.grid_scale : 4.;
     cudaError_t err = cudaSuccess;
     for (int64_t p0 = 0; p0 < L.npts && err == cudaSuccess; p0 += chunk, ++*k)
     {
