@@ -147,3 +147,27 @@ def test_gpu_fdi_host_and_large_batch(cuda):
         assert np.array_equal(h[m], dv[m]), order
     # empty batch is a no-op
     assert bn.fdi_host(1.5, np.empty(0)).size == 0
+
+
+def test_pow_half_accuracy():
+    """x^(h/2) by repeated squaring (times sqrt(x) for odd h), the form of the
+    Sommerfeld regime, stays within a few ulp of the correctly rounded power."""
+    x = np.exp(np.linspace(np.log(100.0), np.log(1e25), 4001))
+    for h in range(-7, 24):
+        got = ft.pow_half(x, h)
+        want = np.power(x, 0.5 * h)
+        ok = np.isfinite(want) & (want > 0)
+        r = np.abs(got[ok] - want[ok]) / want[ok]
+        assert r.max() <= 8 * np.finfo(float).eps, (h, float(r.max()))
+
+
+def test_aux_workload_has_no_reference_arm():
+    import json
+    import subprocess
+    import sys
+    from conftest import REPO
+    out = subprocess.run([sys.executable, "bench.py", "--workload", "aux", "--impl", "reference"],
+                         cwd=REPO, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and "unavailable" in line
