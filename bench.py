@@ -50,6 +50,9 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 SEED = 20261203
+# The metric of both arms (this library and the reference's CPU code); the
+# mixed-vs-FP64 comparison is reported under "fp64_gpu" and "accuracy".
+METRIC = "grey M1 opacity points/s"
 BREM_NAMES = ["HR98", "BRT06", "GP19"]
 WORKLOADS = {
     "c1": dict(npts=4096, flags=(1, 1, 1, 0, 1), brem=0, nq=10,
@@ -90,6 +93,9 @@ def parse():
                     help="skip the spectral leg of the c2/c5 workloads")
     ap.add_argument("--spectral-npts", type=int, default=262144,
                     help="points of the spectral leg (24 energies each)")
+    ap.add_argument("--full-parity", action="store_true",
+                    help="check the FP64 GPU path on every point against the CPU oracle "
+                         "instead of benchmarking")
     ap.add_argument("--cond-npts", type=int, default=262144,
                     help="points of the grey conditioning probe")
     return ap.parse_args()
@@ -167,22 +173,32 @@ def load_json(*path):
         return {}
 
 
-def cpu_rate(eos, m1, wl, n, nthreads):
-    """Reference algorithm (oracle/ C restatement) on host cores: points/s."""
+def cpu_impl():
+    """The CPU implementation timed as the baseline: the reference's own
+    headers built with -O3 for the host CPU and OpenMP (oracle/build_ref.py,
+    kind "reference"), else the C restatement in oracle/ (kind "port")."""
     import oracle
-    port = oracle.port()
-    q = port.gauss_legendre(wl["nq"])
+    oracle.build()
+    r = oracle.ref_native()
+    if r is not None:
+        return r, "reference", "reference headers, g++ -O3 -march/-mcpu=native -fopenmp"
+    return oracle.port(), "port", "C restatement (oracle/bnsn_oracle.c), gcc -O2 -fopenmp"
+
+
+def cpu_rate(impl, eos, m1, wl, n, nthreads):
+    """Reference algorithm on host cores: points/s of the first n points."""
+    q = impl.gauss_legendre(wl["nq"])
     pars = (1, 0, 1, 1, 1, wl["brem"], 1, 0)
     t0 = time.perf_counter()
-    port.m1_opacities(eos[:, :n], m1[:, :n], wl["flags"], pars, q, nthreads=nthreads)
+    impl.m1_opacities(eos[:, :n], m1[:, :n], wl["flags"], pars, q, nthreads=nthreads)
     dt = time.perf_counter() - t0
     return n / dt, dt
 
 
-def cpu_sample_size(eos, m1, wl, seconds, nthreads, cap):
+def cpu_sample_size(impl, eos, m1, wl, seconds, nthreads, cap):
     """Points the CPU processes in about `seconds` (pilot of 8 points/thread)."""
     pilot = min(cap, 8 * nthreads)
-    rate, _ = cpu_rate(eos, m1, wl, pilot, nthreads)
+    rate, _ = cpu_rate(impl, eos, m1, wl, pilot, nthreads)
     return int(max(pilot, min(cap, rate * seconds)))
 
 
@@ -193,58 +209,59 @@ def setup_gp19(bn, wl):
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the reference's CPU implementation on the host cores.
+    Inputs come from the oracle's copy of the seeded generator, so this arm
+    loads nothing from the product library."""
     if rank != 0:
         return
     import oracle
-    oracle.build()
-    import bns_nurates_gb300 as bn
-    from bns_nurates_gb300 import build as libbuild
-    libbuild.build()
     wl = dict(WORKLOADS[args.workload])
     nthreads = os.cpu_count()
     if args.workload == "aux":
         print(json.dumps({"impl": "reference", "unavailable": "the aux workload times library "
                           "kernels only; the reference has no batched form of them"}))
         return
+    impl, kind, how = cpu_impl()
     if args.workload == "c4":
-        run_reference_blocks(args, wl, nthreads)
+        run_reference_blocks(args, wl, nthreads, impl, kind, how)
         return
+    if args.npts:
+        wl["npts"] = args.npts
     cap = min(wl["npts"], 1 << 18)
-    eos, m1 = bn.synthetic_points(SEED, cap)
+    eos, m1 = oracle.port().synthetic_points(SEED, cap)
     per_step = max(2.0, min(args.cpu_seconds, 150.0 / max(1, args.steps + args.warmup)))
-    n = cpu_sample_size(eos, m1, wl, per_step, nthreads, cap)
+    n = cpu_sample_size(impl, eos, m1, wl, per_step, nthreads, cap)
     for _ in range(args.warmup):
-        cpu_rate(eos, m1, wl, min(n, 4 * nthreads), nthreads)
-    rates = [cpu_rate(eos, m1, wl, n, nthreads)[0] for _ in range(args.steps)]
+        cpu_rate(impl, eos, m1, wl, min(n, 4 * nthreads), nthreads)
+    rates = [cpu_rate(impl, eos, m1, wl, n, nthreads)[0] for _ in range(args.steps)]
     value = statistics.median(rates)
     sample = f"first {n} points of the {args.workload} workload per step"
     line = {
-        "impl": "reference", "metric": "grey M1 opacity points/s", "value": value,
+        "impl": "reference", "metric": METRIC, "value": value,
         "unit": "points/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * n / value, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
         "config": {"workload": wl["desc"], "sample_points_per_step": n,
                    "reactions": wl["flags"], "brem": BREM_NAMES[wl["brem"]], "nquad": wl["nq"],
-                   "precision": "fp64 (reference CPU algorithm)"},
-        "cpu_baseline": {"value": value, "unit": "points/s", "cores": nthreads, "kind": "port",
-                         "sample": sample},
+                   "precision": "fp64 (reference CPU algorithm)", "build": how},
+        "cpu_baseline": {"value": value, "unit": "points/s", "cores": nthreads, "kind": kind,
+                         "sample": sample, "build": how},
         "e2e": {"value": value, "unit": "points/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
 
 
-def run_reference_blocks(args, wl, nthreads):
-    """Reference algorithm on the host cores for the AMR-block workload: the
-    oracle per block (its reactions, brem and n) over the leading blocks, up to
-    about --cpu-seconds of work per step."""
+def run_reference_blocks(args, wl, nthreads, impl, kind, how):
+    """Reference algorithm on the host cores for the AMR-block workload: per
+    block (its reactions, brem and n) over the leading blocks, up to about
+    --cpu-seconds of work per step."""
     import oracle
-    import bns_nurates_gb300 as bn
     blocks, n = c4_blocks(SEED, 1536, None)
     cap = min(n, 1 << 17)
-    eos, m1 = bn.synthetic_points(SEED, cap)
+    eos, m1 = oracle.port().synthetic_points(SEED, cap)
     rho = eos[0] * 1.66053906892e-24 * 1e21
-    port = oracle.port()
+    port = impl
 
     def sample(npts):
         done, t0 = 0, time.perf_counter()
@@ -270,14 +287,15 @@ def run_reference_blocks(args, wl, nthreads):
         rates.append(d / dt)
     value = statistics.median(rates)
     print(json.dumps({
-        "impl": "reference", "metric": "grey M1 opacity points/s", "value": value,
+        "impl": "reference", "metric": METRIC, "value": value,
         "unit": "points/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * d / value, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
         "config": {"workload": wl["desc"], "sample": f"leading blocks, ~{target} points per step",
-                   "precision": "fp64 (reference CPU algorithm)"},
-        "cpu_baseline": {"value": value, "unit": "points/s", "cores": nthreads, "kind": "port",
-                         "sample": f"leading blocks of the AMR workload, ~{target} points"},
+                   "precision": "fp64 (reference CPU algorithm)", "build": how},
+        "cpu_baseline": {"value": value, "unit": "points/s", "cores": nthreads, "kind": kind,
+                         "sample": f"leading blocks of the AMR workload, ~{target} points",
+                         "build": how},
         "e2e": {"value": value, "unit": "points/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0}}))
 
@@ -289,6 +307,37 @@ def rel_err(a, b):
     r[a == b] = 0.
     r[~np.isfinite(r)] = np.inf
     return r
+
+
+SPECIES = ("nue", "anue", "nux", "anux")
+GREY_NAMES = [f"{f}[{sp}]" for f in ("eta_0", "kappa_0_a", "eta", "kappa_a", "kappa_s")
+              for sp in SPECIES]
+SPEC_NAMES = [f"{f}[{sp}]" for f in ("j", "kappa", "j_s", "kappa_s") for sp in SPECIES]
+M_U_G = 1.66053906892e-24   # atomic mass unit [g]: rho = nb * m_u * 1e21
+
+
+def degenerate_corner(eos_h):
+    """Points of the degenerate corner T < 2 MeV, rho > 1e14 g/cm^3."""
+    return (eos_h[1] < 2.) & (eos_h[0] * M_U_G * 1e21 > 1e14)
+
+
+def _stats(x):
+    x = np.asarray(x).reshape(-1)
+    if x.size == 0:
+        return None
+    return {"max": float(x.max()), "p99": float(np.percentile(x, 99))}
+
+
+def error_report(r, names, corner):
+    """Max and p99 of the relative error r[output, point, ...] per output, over
+    all points and over the degenerate corner."""
+    rc = r[:, corner]
+    return {
+        "per_output": {nm: _stats(r[k]) for k, nm in enumerate(names)},
+        "degenerate_corner": {"criterion": "T < 2 MeV and rho > 1e14 g/cm^3",
+                              "points": int(corner.sum()), "all_outputs": _stats(rc),
+                              "per_output": {nm: _stats(rc[k]) for k, nm in enumerate(names)}},
+    }
 
 
 def timed_steps(step, steps, stream, torch):
@@ -500,7 +549,8 @@ def run_blocks(args, rank, world, local):
     if rank == 0:
         nq20 = sum(1 for b in blocks if b[4] == 20)
         line = {
-            "metric": "grey M1 opacity points/s, mixed vs FP64 GPU",
+            "metric": METRIC,
+            "comparison": "mixed-precision path vs plain FP64 GPU path (fp64_gpu, accuracy)",
             "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps,
             "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
@@ -524,9 +574,10 @@ def run_blocks(args, rank, world, local):
 
 
 SPEC_ENERGIES = np.logspace(0., np.log10(300.), 24)
+SPEC_WARMUP, SPEC_STEPS = 3, 5
 
 
-def spectral_leg(args, bn, torch, eos, m1, flags, params, q, stream, world, dev):
+def spectral_leg(args, bn, torch, eos, m1, eos_h, flags, params, q, stream, world, dev):
     """Spectral opacities (16 outputs x 24 energies per point) of the first
     --spectral-npts points: device-timed points/s of --precision and, for the
     mixed path, of the plain FP64 path on the same points, the mixed-vs-FP64
@@ -542,14 +593,15 @@ def spectral_leg(args, bn, torch, eos, m1, flags, params, q, stream, world, dev)
             bn.spectral_opacities(eo, mo, flags, params, q, SPEC_ENERGIES, precision=prec,
                                   out=o, stream=stream)
 
-        sstep()
+        for _ in range(SPEC_WARMUP):
+            sstep()
         if prec == "mixed":
             bn.spectral_mixed_stats(reset=True)
-        ms = timed_steps(sstep, 1, stream, torch)
+        ms = timed_steps(sstep, SPEC_STEPS, stream, torch) / SPEC_STEPS
         legs[prec] = {"value": world * ns / (ms * 1e-3), "unit": "points/s", "ms": ms,
-                      "steps": 1, "warmup": 1}
+                      "steps": SPEC_STEPS, "warmup": SPEC_WARMUP}
         if prec == "mixed":
-            st = bn.spectral_mixed_stats(reset=True)
+            st = bn.spectral_mixed_stats(reset=True)   # totals over the SPEC_STEPS calls
             legs[prec]["fp64_recomputed"] = {k: v / max(1, st["evaluated"])
                                              for k, v in st.items() if k != "evaluated"}
         outs[prec] = o
@@ -562,18 +614,19 @@ def spectral_leg(args, bn, torch, eos, m1, flags, params, q, stream, world, dev)
         res["accuracy"] = {"vs": "plain FP64 GPU path, every output, point and energy",
                            "max_rel": float(r.max()), "p99_rel": float(np.percentile(r, 99)),
                            "p999_rel": float(np.percentile(r, 99.9)),
-                           "frac_above_1e-6": float(np.mean(r > 1e-6))}
+                           "frac_above_1e-6": float(np.mean(r > 1e-6)),
+                           **error_report(r, SPEC_NAMES, degenerate_corner(eos_h[:, :ns]))}
 
         def spec64(e, o):
             bn.spectral_opacities(e, mo, flags, params, q, SPEC_ENERGIES, precision="fp64",
                                   out=o, stream=stream)
 
         res["accuracy"].update(conditioned_error(torch, eo, spec64, tuple(outs["fp64"].shape),
-                                                 r, b))
+                                                 r, b, SPEC_NAMES))
     return res
 
 
-def conditioned_error(torch, eos, run64, shape, r, ref):
+def conditioned_error(torch, eos, run64, shape, r, ref, names):
     """Splits the mixed-vs-FP64 error by the conditioning of each output: an
     output is well conditioned when the FP64 path moves by at most 1e-9
     (relative) under a two-ulp change of T or of mu_e; there the contract is
@@ -588,12 +641,98 @@ def conditioned_error(torch, eos, run64, shape, r, ref):
         torch.cuda.synchronize()
         sens = np.maximum(sens, rel_err(o.cpu().numpy(), ref))
     well = sens <= 1e-9
+    rw = np.where(well, r, 0.)
     return {"well_conditioned": {"criterion": "FP64 output moves <= 1e-9 under +2 ulp in T "
                                               "or mu_e",
                                  "points": int(shape[1]), "fraction": float(well.mean()),
-                                 "max_rel": float(np.max(np.where(well, r, 0.))),
+                                 "max_rel": float(rw.max()),
                                  "p999_rel": float(np.percentile(r[well], 99.9))
-                                 if well.any() else None}}
+                                 if well.any() else None,
+                                 "max_rel_per_output": {nm: float(rw[k].max())
+                                                        for k, nm in enumerate(names)}}}
+
+
+def _probe_sens(fn, fn_fma, eos_h, want):
+    """Largest relative change of the oracle under its FMA build and under T or
+    mu_e moved by two ulps: how far the reference's own result is reproducible."""
+    sens = rel_err(fn_fma(eos_h), want)
+    for row in (1, 7):
+        e2 = eos_h.copy()
+        e2[row] *= 1. + 2. ** -51
+        sens = np.maximum(sens, rel_err(fn(e2), want))
+    return sens
+
+
+def _parity_summary(r, sens, names):
+    """Parity figures of GPU-vs-oracle errors r with probe spreads sens."""
+    above = r > 1e-12
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ratio = np.where(above, r / sens, 0.)
+    well = sens <= 1e-13
+    return {
+        "elements": int(r.size), "max_rel": float(r.max()),
+        "frac_within_1e-12": float(1. - above.mean()),
+        "oracle_frac_reproducible_1e-12": float(np.mean(sens <= 1e-12)),
+        "worst_error_to_spread": float(ratio.max()),
+        "well_conditioned": {"criterion": "oracle probe spread <= 1e-13",
+                             "fraction": float(well.mean()),
+                             "max_rel": float(np.max(np.where(well, r, 0.)))},
+        "max_rel_per_output": {nm: float(r[k].max()) for k, nm in enumerate(names)},
+    }
+
+
+def run_full_parity(args):
+    """--full-parity: the plain FP64 GPU path on every point of the workload
+    (c2: the 2,097,152-point 128^3 patch) against the CPU oracle, with the
+    oracle's three conditioning probes; spectral opacities at 24 energies on
+    every 64th point.  Reports the fraction of elements within 1e-12 and the
+    largest ratio of error to probe spread (the smallest safety factor the
+    parity tests could use)."""
+    import torch
+    import oracle
+    import bns_nurates_gb300 as bn
+    from bns_nurates_gb300 import build as libbuild
+    libbuild.build()
+    oracle.build()
+    wl = dict(WORKLOADS[args.workload])
+    n = args.npts or wl["npts"]
+    setup_gp19(bn, wl)
+    port, pfma = oracle.port(), oracle.port_fma()
+    nthreads = os.cpu_count()
+    t0 = time.perf_counter()
+    eos_h, m1_h = bn.synthetic_points(SEED, n)
+    flags, params = bn.opacity_flags(*wl["flags"]), bn.opacity_params(brem_implementation=wl["brem"])
+    q = bn.gauss_legendre(wl["nq"])
+    eos, m1 = torch.from_numpy(eos_h).cuda(), torch.from_numpy(m1_h).cuda()
+    got = bn.m1_opacities(eos, m1, flags, params, q, precision="fp64").cpu().numpy()
+    qo = port.gauss_legendre(wl["nq"])
+    pars = (1, 0, 1, 1, 1, wl["brem"], 1, 0)
+
+    def grey(impl):
+        return lambda e: impl.m1_opacities(e, m1_h, wl["flags"], pars, qo, nthreads=nthreads)
+
+    want = grey(port)(eos_h)
+    sens = _probe_sens(grey(port), grey(pfma), eos_h, want)
+    res = {"workload": wl["desc"], "points": n,
+           "grey": _parity_summary(rel_err(got, want), sens, GREY_NAMES)}
+    # spectral: every 64th point, 24 log-spaced energies 1-300 MeV
+    idx = np.arange(0, n, 64)
+    es, ms_ = np.ascontiguousarray(eos_h[:, idx]), np.ascontiguousarray(m1_h[:, idx])
+    gs = bn.spectral_opacities(torch.from_numpy(es).cuda(), torch.from_numpy(ms_).cuda(), flags,
+                               params, q, SPEC_ENERGIES, precision="fp64").cpu().numpy()
+
+    def spec(impl):
+        return lambda e: impl.spectral(e, ms_, wl["flags"], pars, qo, SPEC_ENERGIES,
+                                       nthreads=nthreads)
+
+    ws = spec(port)(es)
+    ss = _probe_sens(spec(port), spec(pfma), es, ws)
+    res["spectral"] = {"points": int(idx.size), "energies": int(SPEC_ENERGIES.size),
+                       "sample": "every 64th point of the workload",
+                       **_parity_summary(rel_err(gs, ws), ss, SPEC_NAMES)}
+    res["wall_s"] = time.perf_counter() - t0
+    res["cores"] = nthreads
+    print(json.dumps({"full_parity": res}))
 
 
 def main():
@@ -601,6 +740,9 @@ def main():
     rank, world, local = dist_info()
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.full_parity:
+        run_full_parity(args)
         return
     if args.workload == "c4":
         run_blocks(args, rank, world, local)
@@ -680,13 +822,11 @@ def main():
                 "steps": k64, "warmup": 1, "mixed_over_fp64": ms64 / ms_per_step}
         r64 = out64.cpu().numpy()
         r = rel_err(res, r64)
-        names = [f"{f}[{s}]" for f in ("eta_0", "kappa_0_a", "eta", "kappa_a", "kappa_s")
-                 for s in ("nue", "anue", "nux", "anux")]
         accuracy = {"vs": "plain FP64 GPU path, every output of every point",
                     "max_rel": float(r.max()), "p99_rel": float(np.percentile(r, 99)),
                     "p999_rel": float(np.percentile(r, 99.9)),
                     "frac_above_1e-6": float(np.mean(r > 1e-6)),
-                    "max_rel_per_output": {nm: float(r[k].max()) for k, nm in enumerate(names)}}
+                    **error_report(r, GREY_NAMES, degenerate_corner(eos_h))}
         # conditioning of each output: the FP64 path's own change when T or
         # mu_e moves by two ulps, on the first points of the batch
         nc = min(n, args.cond_npts)
@@ -696,7 +836,7 @@ def main():
                             precision="fp64", stream=stream)
 
         accuracy.update(conditioned_error(torch, eos[:, :nc].contiguous(), grey64,
-                                          (20, nc), r[:, :nc], r64[:, :nc]))
+                                          (20, nc), r[:, :nc], r64[:, :nc], GREY_NAMES))
 
     # end to end through the host-buffer C-ABI call, pinned host memory
     e2e = None
@@ -762,21 +902,22 @@ def main():
     # energies 1-300 MeV) on the first points of the step's batch
     spectral = None
     if args.workload in ("c2", "c5") and not args.no_spectral:
-        spectral = spectral_leg(args, bn, torch, eos, m1, flags, params, q, stream, world, dev)
+        spectral = spectral_leg(args, bn, torch, eos, m1, eos_h, flags, params, q, stream, world,
+                                dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        import oracle
-        oracle.build()
+        impl, kind, how = cpu_impl()
         nthreads = os.cpu_count()
-        ns = cpu_sample_size(eos_h, m1_h, wl, args.cpu_seconds, nthreads, n)
-        rate, dt = cpu_rate(eos_h, m1_h, wl, ns, nthreads)
-        cpu = {"value": rate, "unit": "points/s", "cores": nthreads, "kind": "port",
-               "sample": f"first {ns} points of the step's batch, {dt:.1f} s"}
+        ns = cpu_sample_size(impl, eos_h, m1_h, wl, args.cpu_seconds, nthreads, n)
+        rate, dt = cpu_rate(impl, eos_h, m1_h, wl, ns, nthreads)
+        cpu = {"value": rate, "unit": "points/s", "cores": nthreads, "kind": kind,
+               "sample": f"first {ns} points of the step's batch, {dt:.1f} s", "build": how}
 
     if rank == 0:
         line = {
-            "metric": "grey M1 opacity points/s, mixed vs FP64 GPU",
+            "metric": METRIC,
+            "comparison": "mixed-precision path vs plain FP64 GPU path (fp64_gpu, accuracy)",
             "value": value, "unit": "points/s",
             "n_gpus": world, "steps": args.steps, "warmup": warmup,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",

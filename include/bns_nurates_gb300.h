@@ -289,7 +289,7 @@ int bnsn_m1_opacities(const MyQuadrature* quad_1d, const MyQuadrature* quad_2d,
 /* Grey M1 opacities without any device allocation (no counterpart in the
  * reference).  Same arguments and results as bnsn_m1_opacities, but the
  * per-point scratch records live in a static device array inside the library
- * (room for BNSN_NOALLOC_MAX_POINTS points, 24 MiB) instead of the
+ * (room for BNSN_NOALLOC_MAX_POINTS points, 25 MiB) instead of the
  * stream-ordered pool.  It is meant for callers that must not allocate device
  * memory inside the call: codes whose device memory is owned by their own
  * allocator (hydro/AMR frameworks that reserve most of HBM at start-up, where
@@ -300,6 +300,11 @@ int bnsn_m1_opacities(const MyQuadrature* quad_1d, const MyQuadrature* quad_2d,
  *   - The first call on each device looks up the array's address with that
  *     device current (cudaGetSymbolAddress, which may load a module); make
  *     that first call (npts may be 0) before any stream capture.
+ *   - The array's 25 MiB are taken on a device when the library's module is
+ *     loaded there: at that first call under lazy module loading (the CUDA
+ *     default), but at context creation for every process that loads the
+ *     library when CUDA_MODULE_LOADING=EAGER, whether or not it ever calls
+ *     this entry point.
  *   - Nothing in the array needs to start at zero: every scratch value a
  *     kernel reads is written earlier in the same call.
  *   - There is one array per device: calls that overlap in time on one device

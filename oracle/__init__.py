@@ -34,19 +34,19 @@ N_EOS, N_M1, N_DISTR, N_GREY, N_SPEC = 11, 12, 28, 20, 16
 
 def build(force=False):
     """Compile the C oracle (always) and the reference build (when present)."""
-    src = os.path.join(HERE, "bnsn_oracle.c")
+    srcs = [os.path.join(HERE, "bnsn_oracle.c"), os.path.join(HERE, "bnsn_synth.c")]
     hdr = os.path.join(HERE, "bnsn_oracle_consts.h")
     stale = (not os.path.exists(PORT_SO)) or force or max(
-        os.path.getmtime(src), os.path.getmtime(hdr)) > os.path.getmtime(PORT_SO)
+        os.path.getmtime(f) for f in srcs + [hdr]) > os.path.getmtime(PORT_SO)
     if stale:
         subprocess.check_call([
             "gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC",
-            "-shared", src, "-o", PORT_SO, "-lm"])
+            "-shared"] + srcs + ["-o", PORT_SO, "-lm"])
     if stale or not os.path.exists(PORT_FMA_SO):
         fma = ["-mfma"] if platform.machine() in ("x86_64", "AMD64") else []
         subprocess.check_call([
             "gcc", "-std=c11", "-O2", "-ffp-contract=fast", "-fopenmp", "-fPIC",
-            "-shared"] + fma + [src, "-o", PORT_FMA_SO, "-lm"])
+            "-shared"] + fma + srcs + ["-o", PORT_FMA_SO, "-lm"])
     from . import build_ref  # noqa: WPS433 (local import: optional step)
     try:
         build_ref.build()
@@ -150,6 +150,19 @@ class Oracle:
         f.argtypes = [ctypes.c_int64] + [ctypes.c_void_p] * 3
         f(npts, _p(eos), _p(distr), _p(m1))
         return distr, m1
+
+    def synthetic_points(self, seed, n, first=0, nthreads=None):
+        """Port only: the seeded synthetic workload (eos [11, n], m1 [12, n]),
+        bit-identical to the library's bnsn_synthetic_points."""
+        eos = np.zeros((N_EOS, n))
+        m1 = np.zeros((N_M1, n))
+        f = self._f("synthetic_points")
+        f.argtypes = [ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+                      ctypes.c_void_p, ctypes.c_int]
+        f.restype = ctypes.c_int
+        if f(int(seed), int(first), int(n), _p(eos), _p(m1), int(nthreads or os.cpu_count())):
+            raise ValueError("synthetic_points: bad arguments")
+        return eos, m1
 
     # -- unit-level entry points -------------------------------------------
     def fdi(self, k, x):
@@ -269,6 +282,17 @@ def ref():
     if "ref" not in _cache:
         _cache["ref"] = Oracle(REF_SO, "ref_") if os.path.exists(REF_SO) else None
     return _cache["ref"]
+
+
+def ref_native():
+    """The reference's optimised build for timing (``-O3``, native CPU,
+    OpenMP), compiled on first use from the checkout or its staged copy; None
+    where neither exists or the compiler fails."""
+    if "ref_native" not in _cache:
+        from . import build_ref  # noqa: WPS433
+        path = build_ref.build_native()
+        _cache["ref_native"] = Oracle(path, "ref_") if path else None
+    return _cache["ref_native"]
 
 
 def _synthetic_gp19():

@@ -20,16 +20,29 @@ ignored).  Steps:
 
 Flags: ``-O2 -ffp-contract=off`` (no FMA contraction, so results do not depend
 on the host ISA), OpenMP for the batch drivers.
+
+Timing build (``build_native``): the same driver and headers compiled the way
+a user builds the reference for speed, ``-O3 -march=native`` (``-mcpu=native``
+on aarch64) with OpenMP, into ``oracle/_ref/libbnsn_ref_native.so``.  The
+benchmark times it as the CPU baseline.  Because the benchmark host has no
+reference checkout, ``stage()`` keeps a copy of the reference's ``include/``
+headers in the git-ignored ``oracle/_ref/src/include`` (it travels with the
+working tree, never into the repository's history); ``build_native`` compiles
+from the checkout when present, else from that staged copy.
 """
 
+import glob
 import importlib.util
 import os
+import platform
+import shutil
 import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
-REF = os.environ.get("BNSN_REFERENCE_DIR", "/root/reference")
+# The reference checkout: BNSN_REFERENCE_DIR, else a sibling of this repository.
+REF = os.environ.get("BNSN_REFERENCE_DIR") or os.path.join(os.path.dirname(REPO), "reference")
 OUT = os.path.join(HERE, "_ref")
 
 
@@ -69,8 +82,8 @@ def write_gp19_header(path):
         f.write("".join(src))
 
 
-def write_nmax40_header(path):
-    with open(os.path.join(REF, "include", "bns_nurates.hpp")) as f:
+def write_nmax40_header(path, inc):
+    with open(os.path.join(inc, "bns_nurates.hpp")) as f:
         text = f.read()
     old = "#define BS_N_MAX 20"
     if old not in text:
@@ -79,18 +92,71 @@ def write_nmax40_header(path):
         f.write(text.replace(old, "#define BS_N_MAX 40", 1))
 
 
-def build(verbose=False):
-    if not os.path.isdir(os.path.join(REF, "include")):
-        if verbose:
-            print(f"build_ref: reference not present at {REF}; skipped")
+STAGED = os.path.join(OUT, "src", "include")
+NATIVE_SO = os.path.join(OUT, "libbnsn_ref_native.so")
+
+
+def _include_dir():
+    """The reference headers: the checkout, else the staged copy, else None."""
+    for d in (os.path.join(REF, "include"), STAGED):
+        if os.path.isfile(os.path.join(d, "m1_opacities.hpp")):
+            return d
+    return None
+
+
+def stage():
+    """Copy the checkout's include/*.hpp into oracle/_ref/src/include."""
+    src = os.path.join(REF, "include")
+    if not os.path.isdir(src):
         return False
+    os.makedirs(STAGED, exist_ok=True)
+    for f in glob.glob(os.path.join(src, "*.hpp")):
+        dst = os.path.join(STAGED, os.path.basename(f))
+        if os.path.exists(dst):
+            os.chmod(dst, 0o644)
+        shutil.copyfile(f, dst)
+    return True
+
+
+def _generated(inc):
     gen = os.path.join(OUT, "gen")
     gen40 = os.path.join(OUT, "gen40")
     os.makedirs(gen, exist_ok=True)
     os.makedirs(gen40, exist_ok=True)
     write_gp19_header(os.path.join(gen, "GP19Table.hpp"))
-    write_nmax40_header(os.path.join(gen40, "bns_nurates.hpp"))
+    write_nmax40_header(os.path.join(gen40, "bns_nurates.hpp"), inc)
+    return gen, gen40
+
+
+def build_native(verbose=False):
+    """Optimised build of the reference for timing; returns its path or None."""
+    inc = _include_dir()
+    if inc is None:
+        return None
+    drv = os.path.join(HERE, "ref_driver.cpp")
+    if os.path.exists(NATIVE_SO) and os.path.getmtime(NATIVE_SO) >= max(
+            os.path.getmtime(f) for f in glob.glob(os.path.join(inc, "*.hpp")) + [drv]):
+        return NATIVE_SO
+    gen, gen40 = _generated(inc)
+    arch = "-mcpu=native" if platform.machine() in ("aarch64", "arm64") else "-march=native"
+    cmd = ["g++", "-std=c++17", "-O3", arch, "-fopenmp", "-fPIC", "-shared", "-w",
+           "-include", os.path.join(gen40, "bns_nurates.hpp"), "-I", gen, "-I", inc,
+           drv, "-o", NATIVE_SO]
+    if verbose:
+        print(" ".join(cmd))
+    if subprocess.call(cmd) != 0:
+        return None
+    return NATIVE_SO
+
+
+def build(verbose=False):
+    if not os.path.isdir(os.path.join(REF, "include")):
+        if verbose:
+            print(f"build_ref: reference not present at {REF}; skipped")
+        return False
+    stage()
     inc = os.path.join(REF, "include")
+    gen, gen40 = _generated(inc)
     lib = [
         "g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
         "-w", "-include", os.path.join(gen40, "bns_nurates.hpp"),

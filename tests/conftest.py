@@ -6,6 +6,10 @@ import pytest
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(REPO, "tests", "golden")
+# Checkout of the reference (read for its known-answer tables): the
+# BNSN_REFERENCE_DIR environment variable, else a sibling of this repository.
+REF_DIR = os.environ.get("BNSN_REFERENCE_DIR") or os.path.join(os.path.dirname(REPO),
+                                                               "reference")
 if REPO not in sys.path:
     sys.path.insert(0, REPO)
 

@@ -14,9 +14,8 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, golden, rel_err
+from conftest import GOLDEN, REF_DIR, golden, rel_err
 
-REF_DIR = os.environ.get("BNSN_REFERENCE_DIR", "/root/reference")
 kBS_Mu = 1.66053906892e-24
 kBS_Mb = 1.6737747126723517e-24
 kBS_Q = 1.29333251
@@ -219,3 +218,16 @@ def test_layout_fixture_present():
         lay = json.load(f)
     assert lay["MyQuadrature"]["__size__"] == 400
     assert lay["GreyOpacityParams"]["__size__"] > 0
+
+
+def test_oracle_generator_bitwise_equals_library_generator(port, lib):
+    """The oracle's copy of the seeded synthetic workload (used by the
+    benchmark's reference arm, which must not load the product library) is
+    bit-identical to the library's bnsn_synthetic_points, including points far
+    into the 256^3 index range and a 1-point batch."""
+    import bns_nurates_gb300 as bn
+    for seed, n, first in ((20261203, 2048, 0), (7, 513, 16_000_000), (20261203, 1, 1043426)):
+        e_lib, m_lib = bn.synthetic_points(seed, n, first=first)
+        e_or, m_or = port.synthetic_points(seed, n, first=first)
+        assert np.array_equal(e_lib, e_or) and np.array_equal(m_lib, m_or)
+        assert np.isfinite(e_or).all() and np.isfinite(m_or).all()
