@@ -309,6 +309,8 @@ def rel_err(a, b):
     return r
 
 
+# op-count table entry (profiles/op_counts.json) of each grey workload
+OPCOUNT_WORKLOAD = {"c5": "c5", "c3": "c3", "c2": "c3", "c1": "c3"}
 SPECIES = ("nue", "anue", "nux", "anux")
 GREY_NAMES = [f"{f}[{sp}]" for f in ("eta_0", "kappa_0_a", "eta", "kappa_a", "kappa_s")
               for sp in SPECIES]
@@ -882,13 +884,27 @@ def main():
                                f"{bound.upper()} figure",
                 "launch_ms": top_launch_ms, "launches": top_launches,
                 "share_of_step": top_ms / total_ms if total_ms else None}
-    work = c.get(f"{bound}_flop_per_point")
-    if work:
-        ach = work * pts_per_launch / (top_launch_ms * 1e-3) / 1e12
+    # numerator: the reference algorithm's work per point for this phase,
+    # counted by the op-counting build of the reference (oracle/opcount.py ->
+    # profiles/op_counts.json); the phase's executed FLOP on its pipe (ncu
+    # instruction count) is kept beside it
+    opc = load_json("profiles", "op_counts.json").get(OPCOUNT_WORKLOAD.get(args.workload), {})
+    alg = opc.get("phases", {}).get(top, {}).get("work")
+    executed = c.get(f"{bound}_flop_per_point")
+    if alg:
+        ach = alg * pts_per_launch / (top_launch_ms * 1e-3) / 1e12
         roofline["achieved"] = ach
         roofline["frac"] = ach / peak if peak else None
-        roofline["work_per_point"] = work
-        roofline["work_source"] = c.get("source")
+        roofline["work_per_point"] = alg
+        roofline["work_source"] = ("profiles/op_counts.json: reference operations per point "
+                                   "of the reaction this phase computes (FLOP + "
+                                   "transcendental calls, one each)")
+    if executed:
+        ex = executed * pts_per_launch / (top_launch_ms * 1e-3) / 1e12
+        roofline["executed_per_point"] = executed
+        roofline["executed_tflops"] = ex
+        roofline["executed_frac"] = ex / peak if peak else None
+        roofline["executed_source"] = c.get("source")
     if c.get("dram_bytes_per_point"):
         roofline["traffic"] = c["dram_bytes_per_point"] * pts_per_launch
     hbm = peaks.get("hbm_gbs")
