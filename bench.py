@@ -96,6 +96,10 @@ def parse():
     ap.add_argument("--full-parity", action="store_true",
                     help="check the FP64 GPU path on every point against the CPU oracle "
                          "instead of benchmarking")
+    ap.add_argument("--spectral-stride", type=int, default=64,
+                    help="spectral sample of --full-parity: every k-th point")
+    ap.add_argument("--no-grey-parity", action="store_true",
+                    help="--full-parity: spectral part only")
     ap.add_argument("--cond-npts", type=int, default=262144,
                     help="points of the grey conditioning probe")
     return ap.parse_args()
@@ -654,10 +658,13 @@ def conditioned_error(torch, eos, run64, shape, r, ref, names):
                                                         for k, nm in enumerate(names)}}}
 
 
-def _probe_sens(fn, fn_fma, eos_h, want):
-    """Largest relative change of the oracle under its FMA build and under T or
-    mu_e moved by two ulps: how far the reference's own result is reproducible."""
+def _probe_sens(fn, fn_fma, eos_h, want, fn_fdi=None):
+    """Largest relative change of the oracle under its FMA build, its build
+    with Fermi integrals moved by one part in 2^52, and T or mu_e moved by two
+    ulps: how far the reference's own result is reproducible."""
     sens = rel_err(fn_fma(eos_h), want)
+    if fn_fdi is not None:
+        sens = np.maximum(sens, rel_err(fn_fdi(eos_h), want))
     for row in (1, 7):
         e2 = eos_h.copy()
         e2[row] *= 1. + 2. ** -51
@@ -665,13 +672,24 @@ def _probe_sens(fn, fn_fma, eos_h, want):
     return sens
 
 
-def _parity_summary(r, sens, names):
-    """Parity figures of GPU-vs-oracle errors r with probe spreads sens."""
+def _parity_summary(r, sens, names, got=None, want=None, worst=0):
+    """Parity figures of GPU-vs-oracle errors r with probe spreads sens; with
+    worst > 0 also the `worst` elements of largest error-to-spread ratio
+    (index into r, output name, values)."""
     above = r > 1e-12
     with np.errstate(divide="ignore", invalid="ignore"):
         ratio = np.where(above, r / sens, 0.)
     well = sens <= 1e-13
+    top = []
+    if worst:
+        flat = np.argsort(ratio, axis=None)[::-1][:worst]
+        for f in flat:
+            idx = np.unravel_index(f, r.shape)
+            top.append({"index": [int(i) for i in idx], "output": names[idx[0]],
+                        "rel_err": float(r[idx]), "spread": float(sens[idx]),
+                        "gpu": float(got[idx]), "oracle": float(want[idx])})
     return {
+        "worst_elements": top,
         "elements": int(r.size), "max_rel": float(r.max()),
         "frac_within_1e-12": float(1. - above.mean()),
         "oracle_frac_reproducible_1e-12": float(np.mean(sens <= 1e-12)),
@@ -699,7 +717,7 @@ def run_full_parity(args):
     wl = dict(WORKLOADS[args.workload])
     n = args.npts or wl["npts"]
     setup_gp19(bn, wl)
-    port, pfma = oracle.port(), oracle.port_fma()
+    port, pfma, pfdi = oracle.port(), oracle.port_fma(), oracle.port_fdi()
     nthreads = os.cpu_count()
     t0 = time.perf_counter()
     eos_h, m1_h = bn.synthetic_points(SEED, n)
@@ -713,12 +731,13 @@ def run_full_parity(args):
     def grey(impl):
         return lambda e: impl.m1_opacities(e, m1_h, wl["flags"], pars, qo, nthreads=nthreads)
 
-    want = grey(port)(eos_h)
-    sens = _probe_sens(grey(port), grey(pfma), eos_h, want)
-    res = {"workload": wl["desc"], "points": n,
-           "grey": _parity_summary(rel_err(got, want), sens, GREY_NAMES)}
-    # spectral: every 64th point, 24 log-spaced energies 1-300 MeV
-    idx = np.arange(0, n, 64)
+    res = {"workload": wl["desc"], "points": n}
+    if not args.no_grey_parity:
+        want = grey(port)(eos_h)
+        sens = _probe_sens(grey(port), grey(pfma), eos_h, want, grey(pfdi))
+        res["grey"] = _parity_summary(rel_err(got, want), sens, GREY_NAMES, got, want, worst=8)
+    # spectral: every 64th point (--spectral-stride), 24 log-spaced energies 1-300 MeV
+    idx = np.arange(0, n, args.spectral_stride)
     es, ms_ = np.ascontiguousarray(eos_h[:, idx]), np.ascontiguousarray(m1_h[:, idx])
     gs = bn.spectral_opacities(torch.from_numpy(es).cuda(), torch.from_numpy(ms_).cuda(), flags,
                                params, q, SPEC_ENERGIES, precision="fp64").cpu().numpy()
@@ -728,10 +747,11 @@ def run_full_parity(args):
                                        nthreads=nthreads)
 
     ws = spec(port)(es)
-    ss = _probe_sens(spec(port), spec(pfma), es, ws)
+    ss = _probe_sens(spec(port), spec(pfma), es, ws, spec(pfdi))
     res["spectral"] = {"points": int(idx.size), "energies": int(SPEC_ENERGIES.size),
-                       "sample": "every 64th point of the workload",
-                       **_parity_summary(rel_err(gs, ws), ss, SPEC_NAMES)}
+                       "sample": "every 64th point of the workload (index = [output, "
+                                 "sample, energy]; workload point = 64 * sample)",
+                       **_parity_summary(rel_err(gs, ws), ss, SPEC_NAMES, gs, ws, worst=8)}
     res["wall_s"] = time.perf_counter() - t0
     res["cores"] = nthreads
     print(json.dumps({"full_parity": res}))

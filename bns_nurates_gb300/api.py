@@ -238,6 +238,22 @@ def fdi(order, x, out=None, stream=None):
     return out
 
 
+def pair_j_mixed(y, z, eta, stream=None):
+    """The mixed path's pair integrals J_0 = PairPsi(y, z) / (1 - e^{y+z}) and
+    J_1 = PairPsi(z, y) / (1 - e^{y+z}) at float64 CUDA tensors y, z, eta of one
+    shape: (j0, j1, lscale) with J_l = exp(lscale) * j_l."""
+    import torch
+    y, z, eta = (torch.broadcast_tensors(*(t.to(torch.float64) for t in (y, z, eta))))
+    y, z, eta = y.contiguous(), z.contiguous(), eta.contiguous()
+    if not y.is_cuda:
+        raise ValueError("y, z, eta must be CUDA tensors")
+    j0, j1, ls = torch.empty_like(y), torch.empty_like(y), torch.empty_like(y)
+    _check(C.load().bnsn_pair_j_mixed(y.data_ptr(), z.data_ptr(), eta.data_ptr(), j0.data_ptr(),
+                                      j1.data_ptr(), ls.data_ptr(), y.numel(),
+                                      _stream_handle(stream)))
+    return j0, j1, ls
+
+
 def fdi_host(order, x):
     """F_order(x) of a host float64 array (copied to the GPU and back)."""
     k2 = _twice_order(order)

@@ -875,6 +875,21 @@ extern "C" int bnsn_fdi(int twice_order, const double* x, double* out, int64_t n
     return e == cudaSuccess ? BNSN_OK : cuda_fail(e, "fdi kernel launch");
 }
 
+extern "C" int bnsn_pair_j_mixed(const double* y, const double* z, const double* eta, double* j0,
+                                 double* j1, double* lscale, int64_t n, void* stream)
+{
+    g_err.clear();
+    if (n < 0 || (n > 0 && (!y || !z || !eta || !j0 || !j1 || !lscale)))
+        return fail(BNSN_ERR_ARG, "invalid argument");
+    DeviceState* st;
+    int rc = device_state(&st);
+    if (rc)
+        return rc;
+    cudaError_t e = launch_pair_j(y, z, eta, j0, j1, lscale, n, (cudaStream_t)stream,
+                                  st->num_sms);
+    return e == cudaSuccess ? BNSN_OK : cuda_fail(e, "pair integral kernel launch");
+}
+
 extern "C" int bnsn_fdi_host(int twice_order, const double* x, double* out, int64_t n)
 {
     g_err.clear();

@@ -41,6 +41,7 @@
 #include "bnsn_fp32.cuh"
 #include "bnsn_mixed.cuh"
 #include "bnsn_fp64.cuh"
+#include "bnsn_pair32.cuh"
 #include "bnsn_internal.h"
 
 namespace bnsn {
@@ -74,6 +75,21 @@ struct PointTab
 static_assert(sizeof(PointTab) % sizeof(double) == 0, "PointTab must be double words");
 static_assert(sizeof(PointTab) == kGreyRecordBytes, "grey record size");
 constexpr int kTabWords = sizeof(PointTab) / sizeof(double);
+
+// Mixed path with the pair kernel on: the pair phase computes no Fermi-integral
+// tables (fm, fp), so their words hold its own sums, their magnitudes and the
+// final kernel's verdict instead.
+struct PairMixed
+{
+    double spair[16]; // the pair part of s2d
+    double pmag[16];  // sum of |term| of the pair cells per moment (s2d units)
+    double predo;     // 1 if the point's pair sums must be recomputed in FP64
+};
+static_assert(sizeof(PairMixed) <= sizeof(((PointTab*)nullptr)->fm), "PairMixed overlay");
+__device__ __forceinline__ PairMixed* pair_mixed(PointTab* P)
+{
+    return reinterpret_cast<PairMixed*>(&P->fm[0][0]);
+}
 
 size_t grey_point_scratch_bytes() { return sizeof(PointTab); }
 
@@ -253,7 +269,7 @@ __global__ void __launch_bounds__(kWarps * 32)
                 W.y[a]          = nu / T;
                 total_nu_f4(nu, W.d, same_cf, W.g[a]);
             }
-            if (L.use_pair)
+            if (L.use_pair && !L.mixed) // the mixed pair phase needs no F tables
             {
                 for (int qq = lane; qq < 2 * M; qq += 32)
                 {
@@ -522,6 +538,8 @@ __device__ __forceinline__ void beta_in_sum_units(const PointTab* P, double T, d
 constexpr double kMaxCancel = 2.0;
 // FP32 brem cells carry up to ~6e-7 per term (the HR98 fit in FP32).
 constexpr double kMaxCancelBrem = 1.25;
+// FP32 pair integrals carry up to ~3e-7 per cell.
+constexpr double kMaxCancelPair = 1.5;
 // The accurate (all-df) pass keeps ~1e-13 per term.
 constexpr double kMaxCancelDf = 1e5;
 
@@ -589,15 +607,100 @@ __device__ __forceinline__ void fill_tab32(CellTab32& D, const CellTab& C, int M
     }
 }
 
+// Weight algebra of add_cell for the mixed pair cells, with w4 = 1 (the
+// caller folds (nu nubar)^2 into the kernel) and the emission terms'
+// magnitudes: the pair kernels are non-negative and so are the absorption
+// terms (em + am = em (1 + g (e^s - 1)) >= 0), so only the emission terms,
+// through 1 - g < 0, can carry the opposite sign.
+template <bool STIM>
+__device__ __forceinline__ void add_cell_pair(double* acc, double* magem, const double* Kem,
+                                              const double* Kab, const double* ga,
+                                              const double* gb, bool nb_block, double W1,
+                                              double W2)
+{
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+    {
+        const int ps    = s ^ 1;
+        const double bf = nb_block ? 1. : 1. - gb[ps];
+        const double em = Kem[s] * bf;
+        const double am = Kab[s] * gb[ps];
+        double EM, AB, EMA;
+        if (STIM)
+        {
+            AB  = ga[s] * (em + am);
+            EM  = em;
+            EMA = Kem[s] * fabs(bf);
+        }
+        else
+        {
+            AB  = am * ga[s];
+            EM  = em * (1. - ga[s]);
+            EMA = Kem[s] * fabs(bf) * fabs(1. - ga[s]);
+        }
+        acc[s] += EM * W1;
+        acc[4 + s] += AB * W1;
+        acc[8 + s] += EM * W2;
+        acc[12 + s] += AB * W2;
+        magem[s] += EMA * W1;
+        magem[4 + s] += EMA * W2;
+    }
+}
+
+// Per-warp node tables of the mixed pair phase: y = nu/T as double-float,
+// e^{y - |eta|/2} (e^{Lref} = its product over the two nodes when |eta| >= s)
+// and e^{-y} (e^{-s} = the product when s <= 700).
+struct PairTab32
+{
+    float yh[kMaxM], yl[kMaxM];
+    double eh[kMaxM], dn[kMaxM];
+};
+
+// Pair cell (a, b) of the mixed path: Psi_0(y, z) and Psi_0(z, y) from the
+// cancellation-free FP32 integral (bnsn_pair32.cuh); em and ab of
+// kernel_pair.hpp:135-198 times (nu nubar)^2: ab = e^{s} em =
+// (Phi T^2 / 2) alpha . (Psi / (1 - e^s)) e^{s}, em = ab / SafeExp(s).
+// sc = (Phi T^2 / 2) T^4 / 15 (the point's factor).
+__device__ __forceinline__ void pair_kernel_q(const PairTab32& X, int a, int b, dfm::df ETA,
+                                              double sc, double* em, double* ab)
+{
+    pair32::Cell c;
+    int lcase;
+    const dfm::df Ya = {X.yh[a], X.yl[a]}, Yb = {X.yh[b], X.yl[b]};
+    if (!pair32::make_cell(Ya, Yb, ETA, c, lcase))
+    {
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            em[q] = ab[q] = 0.;
+        return;
+    }
+    double Q0, Q1;
+    pair32::cell_integrals(c, Q0, Q1);
+    const double f = lcase == pair32::kLrefZero ? sc : sc * (X.eh[a] * X.eh[b]);
+    ab[0] = f * ((k::PairA1e * k::PairA1e) * Q0 + (k::PairA2e * k::PairA2e) * Q1);
+    ab[1] = f * ((k::PairA1e * k::PairA1e) * Q1 + (k::PairA2e * k::PairA2e) * Q0);
+    ab[2] = f * ((k::PairA1x * k::PairA1x) * Q0 + (k::PairA2x * k::PairA2x) * Q1);
+    ab[3] = f * ((k::PairA1x * k::PairA1x) * Q1 + (k::PairA2x * k::PairA2x) * Q0);
+    const double ems = c.S.hi <= 700.f ? X.dn[a] * X.dn[b] : 9.8596765437597708e-305; // e^-700
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        em[q] = ab[q] * ems;
+}
+
+// MIXED: pair cells from the FP32 integral; the sums, their magnitudes and
+// s2d are written to the record (PairMixed).  !MIXED: the FP64 pair kernel
+// (kernel_pair.hpp), with redo_only the mixed path's second pass over the
+// points the final kernel marked (predo), whose pair part of s2d it replaces;
+// that pass computes its Fermi-integral tables itself.
 template <bool MIXED>
 __global__ void __launch_bounds__(kWarps * 32)
     grey_pair_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
-                     double* __restrict__ scratch)
+                     double* __restrict__ scratch, int redo_only)
 {
     __shared__ double s_A1[kMaxM], s_A2[kMaxM];
     __shared__ uint32_t s_cells[kMaxCells];
     __shared__ CellTab s_ct[kWarps];
-    __shared__ CellTab32 s_c32[MIXED ? kWarps : 1];
+    __shared__ PairTab32 s_pt[MIXED ? kWarps : 1];
     for (int k = threadIdx.x; k < kMaxM; k += blockDim.x)
     {
         s_A1[k]  = L.A1[k];
@@ -609,6 +712,7 @@ __global__ void __launch_bounds__(kWarps * 32)
     const int lane = threadIdx.x & 31;
     const int wid  = threadIdx.x >> 5;
     CellTab& C     = s_ct[wid];
+    PairTab32& X   = s_pt[MIXED ? wid : 0];
     const int M    = 2 * L.n2;
     const bool nbb = L.neglect_blocking != 0;
     const int64_t nwarp = (int64_t)gridDim.x * kWarps;
@@ -617,55 +721,135 @@ __global__ void __launch_bounds__(kWarps * 32)
     {
         const int64_t p  = L.pidx ? L.pidx[p0 + q] : p0 + q;
         PointTab* P      = (PointTab*)(scratch + q * kTabWords);
+        if (!MIXED && redo_only && pair_mixed(P)->predo != 1.)
+            continue;
         const double T   = L.eos[1][p];
         const double eta = L.eos[7][p] / T;
         __syncwarp();
-        load_cell_tab(C, P, M, true, lane);
+        load_cell_tab(C, P, M, !MIXED && !redo_only, lane);
+        if (MIXED)
+        {
+            __syncwarp();
+            for (int a = lane; a < M; a += 32)
+            {
+                const double y = C.y[a];
+                const dfm::df yd = dfm::from_double(y);
+                X.yh[a] = yd.hi;
+                X.yl[a] = yd.lo;
+                X.eh[a] = exp(y - 0.5 * fabs(eta));
+                X.dn[a] = exp(-y);
+            }
+        }
+        if (!MIXED && redo_only)
+        {
+            // the F_1..F_5 tables the mixed prelude left out
+            for (int qq = lane; qq < 2 * M; qq += 32)
+            {
+                const int a = qq >> 1;
+                if (qq & 1)
+                    fdi_orders<1, 5>(eta + C.y[a], C.fp[a]);
+                else
+                    fdi_orders<1, 5>(eta - C.y[a], C.fm[a]);
+            }
+        }
         __syncwarp();
-        double acc[16];
+        __syncwarp();
+        double acc[16], magem[MIXED ? 8 : 1];
 #pragma unroll
         for (int kk = 0; kk < 16; ++kk)
             acc[kk] = 0.;
+#pragma unroll
+        for (int kk = 0; kk < (MIXED ? 8 : 1); ++kk)
+            magem[kk] = 0.;
+        const dfm::df ETA = dfm::from_double(eta);
+        const double T2 = T * T;
+        const double scq = 0.5 * k::PairPhi * T2 * (T2 * T2) / 15.;
         for (int c = lane; c < L.ncell; c += 32)
         {
             const uint32_t ab = s_cells[c];
             const int a = ab & 0xffffu, b = ab >> 16;
             const double nua = C.nu[a], nub = C.nu[b];
             double pe[4], pa[4];
-            // the pair kernel goes negative in some cells (truncated Legendre
-            // expansion), so its weighted sums stay FP64 in both paths
             if (MIXED)
-                pair_kernel_one_exp(T, eta, C.y[a], C.y[b], C.fm[a], C.fp[a], C.fm[b], C.fp[b],
-                                    C.f3e, C.f4e, pe, pa);
+                pair_kernel_q(X, a, b, ETA, scq, pe, pa);
             else
                 pair_kernel(T, eta, nua, nub, C.y[a], C.y[b], C.fm[a], C.fp[a], C.fm[b],
                             C.fp[b], C.f3e, C.f4e, pe, pa);
             const double w4 = (nua * nua) * (nub * nub);
             const double W1 = s_A1[a] * s_A1[b];
-            if (L.stim)
-                add_cell<true>(acc, pe, pa, C.g[a], C.g[b], nbb, w4, W1, s_A2[a] * s_A1[b]);
-            else
-                add_cell<false>(acc, pe, pa, C.g[a], C.g[b], nbb, w4, W1, s_A2[a] * s_A1[b]);
-            if (a != b)
+            // (b, a): the inverse kernel swaps partner species (kernel_pair.hpp:200-216)
+            const double qe[4] = {pe[1], pe[0], pe[3], pe[2]};
+            const double qa[4] = {pa[1], pa[0], pa[3], pa[2]};
+            if (MIXED)
             {
-                // (b, a): the inverse kernel swaps partner species
-                // (kernel_pair.hpp:200-216)
-                const double qe[4] = {pe[1], pe[0], pe[3], pe[2]};
-                const double qa[4] = {pa[1], pa[0], pa[3], pa[2]};
                 if (L.stim)
-                    add_cell<true>(acc, qe, qa, C.g[b], C.g[a], nbb, w4, W1, s_A2[b] * s_A1[a]);
+                    add_cell_pair<true>(acc, magem, pe, pa, C.g[a], C.g[b], nbb, W1,
+                                        s_A2[a] * s_A1[b]);
                 else
-                    add_cell<false>(acc, qe, qa, C.g[b], C.g[a], nbb, w4, W1, s_A2[b] * s_A1[a]);
+                    add_cell_pair<false>(acc, magem, pe, pa, C.g[a], C.g[b], nbb, W1,
+                                         s_A2[a] * s_A1[b]);
+                if (a != b)
+                {
+                    if (L.stim)
+                        add_cell_pair<true>(acc, magem, qe, qa, C.g[b], C.g[a], nbb, W1,
+                                            s_A2[b] * s_A1[a]);
+                    else
+                        add_cell_pair<false>(acc, magem, qe, qa, C.g[b], C.g[a], nbb, W1,
+                                             s_A2[b] * s_A1[a]);
+                }
+            }
+            else
+            {
+                if (L.stim)
+                    add_cell<true>(acc, pe, pa, C.g[a], C.g[b], nbb, w4, W1, s_A2[a] * s_A1[b]);
+                else
+                    add_cell<false>(acc, pe, pa, C.g[a], C.g[b], nbb, w4, W1, s_A2[a] * s_A1[b]);
+                if (a != b)
+                {
+                    if (L.stim)
+                        add_cell<true>(acc, qe, qa, C.g[b], C.g[a], nbb, w4, W1,
+                                       s_A2[b] * s_A1[a]);
+                    else
+                        add_cell<false>(acc, qe, qa, C.g[b], C.g[a], nbb, w4, W1,
+                                        s_A2[b] * s_A1[a]);
+                }
             }
         }
+        double magd[16];
 #pragma unroll
         for (int kk = 0; kk < 16; ++kk)
             acc[kk] = warp_sum(acc[kk]);
+        if (MIXED)
+        {
+            // emission moments: sum of |term|; absorption terms are non-negative
+#pragma unroll
+            for (int s = 0; s < 4; ++s)
+            {
+                magd[s]      = warp_sum(magem[s]);
+                magd[8 + s]  = warp_sum(magem[4 + s]);
+                magd[4 + s]  = fabs(acc[4 + s]);
+                magd[12 + s] = fabs(acc[12 + s]);
+            }
+        }
         if (lane == 0)
         {
+            PairMixed* X = pair_mixed(P);
 #pragma unroll
             for (int kk = 0; kk < 16; ++kk)
-                P->s2d[kk] = acc[kk];
+            {
+                if (MIXED)
+                {
+                    P->s2d[kk]   = acc[kk];
+                    X->spair[kk] = acc[kk];
+                    X->pmag[kk]  = magd[kk];
+                }
+                else if (redo_only)
+                    P->s2d[kk] = P->s2d[kk] - X->spair[kk] + acc[kk];
+                else
+                    P->s2d[kk] = acc[kk];
+            }
+            if (MIXED)
+                X->predo = 0.;
         }
     }
 }
@@ -1554,13 +1738,17 @@ __global__ void __launch_bounds__(128)
         bool nonfinite      = false;
         const int64_t p     = L.pidx ? L.pidx[p0 + q] : p0 + q;
         PointTab* P         = (PointTab*)(scratch + q * kTabWords);
-        if (redo_only && P->bredo != 1.)
+        const bool pcheck   = L.mixed && L.use_pair;
+        if (redo_only && P->bredo != 1. && !(pcheck && pair_mixed(P)->predo == 1.))
             continue;
         // mixed path: FP32 brem terms whose sum the other reactions cancel
         // (the NES sums of the opposite sign where the occupation exceeds 1)
-        // by more than kMaxCancelBrem are recomputed in FP64 (bredo = 1)
+        // by more than kMaxCancelBrem are recomputed in FP64 (bredo = 1); the
+        // same for the FP32 pair integrals beyond kMaxCancelPair (predo = 1)
         const bool check = !redo_only && L.mixed && L.use_brem;
+        const bool check_pair = !redo_only && pcheck;
         bool bredo       = false;
+        bool predo       = false;
         const double T      = L.eos[1][p];
         const double eta_e  = L.eos[7][p] / T;
         const double t2d    = k::TempMultiple * T;
@@ -1619,17 +1807,21 @@ __global__ void __launch_bounds__(128)
                 o[3] = (J > k::ThresholdJ) ? F2 / (c * J) * (e2d_ab + ene_ab) : 0.;
             }
             o[4] = (J > k::ThresholdJ) ? F / (c * J) * iso : 0.;
-            if (check)
+            if (check || check_pair)
             {
                 // totals of the four moments before the output factors, and the
-                // brem terms' magnitude in the same units
+                // brem (pair) terms' magnitude in the same units
                 const double tot[4] = {F * (n2d_em + nne_em) + bne, F * (n2d_ab + nne_ab) + bna,
                                        F * (e2d_em + ene_em) + bje, F * (e2d_ab + ene_ab) + bja};
 #pragma unroll
                 for (int m = 0; m < 4; ++m)
                 {
-                    const double mag = F * P->bmag[4 * m + s] * (m < 2 ? t2 : t2d * t2);
-                    bredo = bredo || mag > kMaxCancelBrem * fabs(tot[m]);
+                    const double u = F * (m < 2 ? t2 : t2d * t2);
+                    if (check)
+                        bredo = bredo || u * P->bmag[4 * m + s] > kMaxCancelBrem * fabs(tot[m]);
+                    if (check_pair)
+                        predo = predo ||
+                                u * pair_mixed(P)->pmag[4 * m + s] > kMaxCancelPair * fabs(tot[m]);
                 }
             }
 #pragma unroll
@@ -1641,6 +1833,8 @@ __global__ void __launch_bounds__(128)
         }
         if (check)
             P->bredo = bredo ? 1. : 0.;
+        if (check_pair)
+            pair_mixed(P)->predo = predo ? 1. : 0.;
         if (nonfinite && !redo_only)
             atomicAdd(&g_grey_nonfinite, 1ull);
     }
@@ -1686,6 +1880,52 @@ cudaError_t launch_brem(const OpacityLaunch& L, int64_t p0, int64_t np, double* 
 }
 
 } // namespace
+
+namespace {
+
+// The mixed path's pair integrals at given (y, z, eta): J_l = e^{ls} j_l with
+// J_0 = Psi_0(y, z) / (1 - e^{y+z}), J_1 = Psi_0(z, y) / (1 - e^{y+z})
+// (kernel_pair.hpp:16-120), ls = Lref - (y + z).  Zero where the reference
+// zeroes Psi (eta - y - z > 200).
+__global__ void __launch_bounds__(128)
+    pair_j_kernel(const double* __restrict__ y, const double* __restrict__ z,
+                  const double* __restrict__ eta, double* __restrict__ j0,
+                  double* __restrict__ j1, double* __restrict__ ls, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+    {
+        pair32::Cell c;
+        double lref;
+        if (!pair32::make_cell(y[i], z[i], eta[i], c, lref))
+        {
+            j0[i] = j1[i] = 0.;
+            ls[i] = 0.;
+            continue;
+        }
+        double Q0, Q1;
+        pair32::cell_integrals(c, Q0, Q1);
+        const double yz = y[i] * z[i];
+        j0[i] = Q0 / (15. * (yz * yz));
+        j1[i] = Q1 / (15. * (yz * yz));
+        ls[i] = lref - (y[i] + z[i]);
+    }
+}
+
+} // namespace
+
+cudaError_t launch_pair_j(const double* y, const double* z, const double* eta, double* j0,
+                          double* j1, double* ls, int64_t n, cudaStream_t st, int sms)
+{
+    if (n <= 0)
+        return cudaSuccess;
+    const int64_t blocks = (n + 127) / 128;
+    const int grid       = (int)(blocks < (int64_t)sms * 8 ? blocks : (int64_t)sms * 8);
+    phase_mark(kPhAux, 0, st);
+    pair_j_kernel<<<grid, 128, 0, st>>>(y, z, eta, j0, j1, ls, n);
+    phase_mark(kPhAux, 1, st);
+    return cudaGetLastError();
+}
 
 cudaError_t grey_nonfinite_count(unsigned long long* count, bool reset)
 {
@@ -1736,10 +1976,10 @@ cudaError_t launch_grey_chunks(const OpacityLaunch& L, cudaStream_t st0, cudaStr
             phase_mark(kPhPair, 0, st);
             if (L.mixed)
                 grey_pair_kernel<true><<<grid_for(grey_pair_kernel<true>, kWarps * 32, wb, sms),
-                                         kWarps * 32, 0, st>>>(L, p0, np, wsk);
+                                         kWarps * 32, 0, st>>>(L, p0, np, wsk, 0);
             else
                 grey_pair_kernel<false><<<grid_for(grey_pair_kernel<false>, kWarps * 32, wb, sms),
-                                          kWarps * 32, 0, st>>>(L, p0, np, wsk);
+                                          kWarps * 32, 0, st>>>(L, p0, np, wsk, 0);
             phase_mark(kPhPair, 1, st);
         }
         if (L.use_brem)
@@ -1782,10 +2022,19 @@ cudaError_t launch_grey_chunks(const OpacityLaunch& L, cudaStream_t st0, cudaStr
         grey_final_kernel<<<grid_for(grey_final_kernel, 128, (np + 127) / 128, sms), 128, 0, st>>>(
             L, p0, np, wsk, 0);
         phase_mark(kPhFinal, 1, st);
-        if (L.mixed && L.use_brem)
+        if (L.mixed && (L.use_brem || L.use_pair))
         {
-            // points whose FP32 brem sums the NES sums cancel: brem in FP64, outputs again
-            if ((err = launch_brem<false>(L, p0, np, wsk, st, sms, L.use_pair, 1)) != cudaSuccess)
+            // points whose FP32 brem or pair sums the other reactions cancel:
+            // those parts in FP64, outputs again
+            if (L.use_pair)
+            {
+                phase_mark(kPhPair, 0, st);
+                grey_pair_kernel<false><<<grid_for(grey_pair_kernel<false>, kWarps * 32, wb, sms),
+                                          kWarps * 32, 0, st>>>(L, p0, np, wsk, 1);
+                phase_mark(kPhPair, 1, st);
+            }
+            if (L.use_brem &&
+                (err = launch_brem<false>(L, p0, np, wsk, st, sms, L.use_pair, 1)) != cudaSuccess)
                 break;
             phase_mark(kPhFinal, 0, st);
             grey_final_kernel<<<grid_for(grey_final_kernel, 128, (np + 127) / 128, sms), 128, 0,

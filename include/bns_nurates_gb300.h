@@ -454,6 +454,18 @@ int bnsn_m1_opacities_host(const MyQuadrature* quad_1d,
 int bnsn_fdi(int twice_order, const double* x, double* out, int64_t n, void* stream);
 int bnsn_fdi_host(int twice_order, const double* x, double* out, int64_t n);
 
+/* The mixed path's pair-annihilation integrals at n given (y, z, eta), device
+ * arrays, stream-ordered: J_0 = PairPsi(y, z) / (1 - e^{y+z}) and
+ * J_1 = PairPsi(z, y) / (1 - e^{y+z}) of kernel_pair.hpp:16-120 (y = omega/T,
+ * z = omega'/T, eta = mu_e/T; l = 0), returned as J_l = exp(lscale) * j_l so
+ * that values far below the double range stay representable.  The mixed grey
+ * path computes them as a positive FP32 integral over the e- energy instead of
+ * the reference's cancelling Fermi-integral combination; this entry exposes
+ * that integral for testing.  j_l = 0 where the reference zeroes PairPsi
+ * (eta - y - z > 200). */
+int bnsn_pair_j_mixed(const double* y, const double* z, const double* eta, double* j0,
+                      double* j1, double* lscale, int64_t n, void* stream);
+
 /* Gauss-Legendre nodes/weights of order quad->nx on [0,1]; replaces
  * GaussLegendre (integration.hpp:28-87), same algorithm. */
 int bnsn_gauss_legendre(MyQuadrature* quad);

@@ -26,6 +26,11 @@ PORT_SO = os.path.join(HERE, "libbnsn_oracle.so")
 # not reproducible to the last bits (cancellation), which the GPU parity
 # tests use as the per-element conditioning of each output.
 PORT_FMA_SO = os.path.join(HERE, "libbnsn_oracle_fma.so")
+# Same source with every Fermi integral moved by one part in 2^52 (a bit of
+# its argument picks the sign): the reference's sensitivity to an equally
+# accurate evaluation of its Fermi integrals, which the catastrophic
+# cancellation of the pair Psi polynomial at small y, z amplifies.
+PORT_FDI_SO = os.path.join(HERE, "libbnsn_oracle_fdi.so")
 REF_SO = os.path.join(HERE, "_ref", "libbnsn_ref.so")
 REF_LAYOUT = os.path.join(HERE, "_ref", "ref_layout")
 
@@ -47,6 +52,10 @@ def build(force=False):
         subprocess.check_call([
             "gcc", "-std=c11", "-O2", "-ffp-contract=fast", "-fopenmp", "-fPIC",
             "-shared"] + fma + srcs + ["-o", PORT_FMA_SO, "-lm"])
+    if stale or not os.path.exists(PORT_FDI_SO):
+        subprocess.check_call([
+            "gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
+            "-DORACLE_FDI_JITTER"] + srcs + ["-o", PORT_FDI_SO, "-lm"])
     from . import build_ref  # noqa: WPS433 (local import: optional step)
     try:
         build_ref.build()
@@ -275,6 +284,18 @@ def port_fma():
         o.set_gp19_table(_synthetic_gp19())
         _cache["port_fma"] = o
     return _cache["port_fma"]
+
+
+def port_fdi():
+    """The C restatement with its Fermi integrals moved by one part in 2^52
+    (conditioning probe)."""
+    if "port_fdi" not in _cache:
+        if not os.path.exists(PORT_FDI_SO):
+            build()
+        o = Oracle(PORT_FDI_SO, "oracle_")
+        o.set_gp19_table(_synthetic_gp19())
+        _cache["port_fdi"] = o
+    return _cache["port_fdi"]
 
 
 def ref():

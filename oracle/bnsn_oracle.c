@@ -96,6 +96,24 @@ static double horner(const double* c, int deg, double t)
  * Regimes in x = -|y|: x < -2 (series in e^x), -2 <= x <= 0 (rational in
  * s = -x/2), and y > 0 through the reflection polynomial. NaN gives 0. */
 
+/* Conditioning probe (ORACLE_FDI_JITTER builds only): each Fermi integral
+ * moved by one part in 2^52, up or down by a bit of its argument, as a
+ * different but equally accurate evaluation of the same approximation would
+ * (another compiler's FMA contraction of the Horner steps).  Where the
+ * reference combines the integrals with catastrophic cancellation (the pair
+ * Psi polynomial at small y, z) this is how far its own result is
+ * reproducible; the FMA build and small input changes do not show it. */
+#ifdef ORACLE_FDI_JITTER
+static double fdi_jitter(double fd, double y)
+{
+    uint64_t b;
+    memcpy(&b, &y, sizeof(b));
+    return fd * (1. + (((b >> 7) & 1u) ? 0x1p-52 : -0x1p-52));
+}
+#else
+#define fdi_jitter(fd, y) (fd)
+#endif
+
 /* functions.hpp:1550-1612 */
 static double fdi_0(double y)
 {
@@ -128,7 +146,7 @@ static double fdi_0(double y)
     }
     if (y > 0.)
         fd = fd + y;
-    return fd;
+    return fdi_jitter(fd, y);
 }
 
 /* functions.hpp:1795-1860 */
@@ -164,7 +182,7 @@ static double fdi_p1(double y)
     }
     if (y > 0.)
         fd = -fd + 1.64493406684822644 + 0.5 * y * y;
-    return fd;
+    return fdi_jitter(fd, y);
 }
 
 /* functions.hpp:2051-2112 */
@@ -199,7 +217,7 @@ static double fdi_p2(double y)
     }
     if (y > 0.)
         fd = fd + y * (3.28986813369645287 + 0.333333333333333333 * y * y);
-    return fd;
+    return fdi_jitter(fd, y);
 }
 
 /* functions.hpp:2293-2350 */
@@ -236,7 +254,7 @@ static double fdi_p3(double y)
         const double y2 = y * y;
         fd = -fd + 11.3643939539669510 + y2 * (4.93480220054467931 + y2 * 0.25);
     }
-    return fd;
+    return fdi_jitter(fd, y);
 }
 
 /* functions.hpp:2535-2592 */
@@ -274,7 +292,7 @@ static double fdi_p4(double y)
         fd = fd + y * (45.4575758158678040 +
                        y2 * (6.57973626739290575 + y2 * 0.2));
     }
-    return fd;
+    return fdi_jitter(fd, y);
 }
 
 /* functions.hpp:2778-2838 */
@@ -313,7 +331,7 @@ static double fdi_p5(double y)
              y2 * (113.643939539669510 +
                    y2 * (8.22467033424113218 + y2 * 0.166666666666666667));
     }
-    return fd;
+    return fdi_jitter(fd, y);
 }
 
 /* functions.hpp:4376-4396: Fermi-Dirac occupation, split on the sign of

@@ -3,8 +3,9 @@
 Contract: at most 1e-6 relative error per emissivity and opacity against the
 FP64 oracle, on every output the reference itself computes reproducibly.
 An element's reproducibility is the largest deviation of the oracle under
-three O(eps) perturbations (the FMA build of the same code, and T or mu_e
-moved by two ulps).  Where that deviation is at most 1e-9 the element is well
+four O(eps) perturbations (the FMA build of the same code, the build whose
+Fermi integrals are moved by one part in 2^52, and T or mu_e moved by two
+ulps).  Where that deviation is at most 1e-9 the element is well
 conditioned and must be within MIXED_TOL; elsewhere the reference's own
 result moves by more than the mixed path's rounding would explain, and the
 bound is COND_MIXED times that deviation (never below MIXED_TOL).
@@ -32,6 +33,11 @@ def port_fma():
     return oracle.port_fma()
 
 
+def _port_fdi():
+    import oracle
+    return oracle.port_fdi()
+
+
 def _params(pars):
     return bn.opacity_params(*[bool(v) for v in pars[:5]], brem_implementation=int(pars[5]),
                              use_NN_medium_corr=bool(pars[6]), neglect_blocking=bool(pars[7]))
@@ -53,6 +59,8 @@ def _oracle_with_sens(port, port_fma, eos, m1, flags, pars, nq, stim=1, distr=No
     kw = dict(distr=distr, stim_abs=stim, nthreads=NTHREADS)
     want = port.m1_opacities(eos, m1, flags, pars, q, **kw)
     sens = rel_err(port_fma.m1_opacities(eos, m1, flags, pars, q, **kw), want, floor=1e-300)
+    sens = np.maximum(sens, rel_err(_port_fdi().m1_opacities(eos, m1, flags, pars, q, **kw),
+                                    want, floor=1e-300))
     for row in (1, 7):
         e2 = np.array(eos, copy=True)
         e2[row] *= 1. + 2. ** -51
@@ -84,6 +92,8 @@ CASES = [
     ("beta+iso+pair+HR98, n=10", (1, 1, 1, 0, 1), (1, 0, 1, 1, 1, 0, 1, 0), 10, 1),
     ("NES only, n=20, not stimulated", (0, 0, 0, 1, 0), (1, 0, 1, 1, 1, 0, 1, 0), 20, 0),
     ("pair+BRT06, n=8, neglect blocking", (0, 1, 1, 0, 0), (0, 1, 0, 0, 0, 1, 0, 1), 8, 1),
+    ("pair only, n=20", (0, 1, 0, 0, 0), (1, 0, 1, 1, 1, 0, 1, 0), 20, 1),
+    ("pair only, n=10, not stimulated", (0, 1, 0, 0, 0), (1, 0, 1, 1, 1, 0, 1, 0), 10, 0),
     ("GP19 brem only, n=12, no medium", (0, 0, 1, 0, 0), (1, 0, 1, 1, 1, 2, 0, 0), 12, 1),
 ]
 
@@ -129,6 +139,8 @@ def _spec_oracle_with_sens(port, port_fma, eos, m1, flags, pars, nq, energies, s
     want = port.spectral(eos, m1, flags, pars, q, energies, **kw)
     sens = rel_err(port_fma.spectral(eos, m1, flags, pars, q, energies, **kw), want,
                    floor=1e-300)
+    sens = np.maximum(sens, rel_err(_port_fdi().spectral(eos, m1, flags, pars, q, energies,
+                                                         **kw), want, floor=1e-300))
     for row in (1, 7):
         e2 = np.array(eos, copy=True)
         e2[row] *= 1. + 2. ** -51
