@@ -163,6 +163,7 @@ SIGNATURES = {
     "bnsn_nonfinite_outputs": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64), ctypes.c_int]),
     "bnsn_fdi": (c_int, [c_int, P, P, ctypes.c_int64, P]),
     "bnsn_pair_j_mixed": (c_int, [P, P, P, P, P, P, ctypes.c_int64, P]),
+    "bnsn_nes_m_mixed": (c_int, [P, P, P, P, P, P, ctypes.c_int64, P]),
     "bnsn_fdi_host": (c_int, [c_int, P, P, ctypes.c_int64]),
     "bnsn_status_string": (ctypes.c_char_p, [c_int]),
     "bnsn_last_error": (ctypes.c_char_p, []),

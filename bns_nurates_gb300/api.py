@@ -254,6 +254,22 @@ def pair_j_mixed(y, z, eta, stream=None):
     return j0, j1, ls
 
 
+def nes_m_mixed(w, wp, eta, stream=None):
+    """The mixed path's NES/NPS out-kernel integrals: MezzacappaIntOut(w, w',
+    b1, b2) = exp(lscale) * (b1 m1 + b2 m2) at float64 CUDA tensors w, w', eta
+    of one shape: (m1, m2, lscale)."""
+    import torch
+    w, wp, eta = (torch.broadcast_tensors(*(t.to(torch.float64) for t in (w, wp, eta))))
+    w, wp, eta = w.contiguous(), wp.contiguous(), eta.contiguous()
+    if not w.is_cuda:
+        raise ValueError("w, wp, eta must be CUDA tensors")
+    m1, m2, ls = torch.empty_like(w), torch.empty_like(w), torch.empty_like(w)
+    _check(C.load().bnsn_nes_m_mixed(w.data_ptr(), wp.data_ptr(), eta.data_ptr(), m1.data_ptr(),
+                                     m2.data_ptr(), ls.data_ptr(), w.numel(),
+                                     _stream_handle(stream)))
+    return m1, m2, ls
+
+
 def fdi_host(order, x):
     """F_order(x) of a host float64 array (copied to the GPU and back)."""
     k2 = _twice_order(order)

@@ -140,6 +140,8 @@ struct EquilLaunch
 cudaError_t launch_distr_from_m1(const DistrLaunch& L, cudaStream_t stream, int num_sms);
 // Fermi-Dirac integral F_{k2/2} of n arguments (device arrays).
 bool fdi_order_valid(int k2);
+cudaError_t launch_nes_m(const double* w, const double* wp, const double* eta, double* m1,
+                         double* m2, double* ls, int64_t n, cudaStream_t stream, int num_sms);
 cudaError_t launch_pair_j(const double* y, const double* z, const double* eta, double* j0,
                           double* j1, double* ls, int64_t n, cudaStream_t stream, int num_sms);
 cudaError_t launch_fdi(int k2, const double* x, double* out, int64_t n, cudaStream_t stream,

@@ -890,6 +890,21 @@ extern "C" int bnsn_pair_j_mixed(const double* y, const double* z, const double*
     return e == cudaSuccess ? BNSN_OK : cuda_fail(e, "pair integral kernel launch");
 }
 
+extern "C" int bnsn_nes_m_mixed(const double* w, const double* wp, const double* eta, double* m1,
+                                double* m2, double* lscale, int64_t n, void* stream)
+{
+    g_err.clear();
+    if (n < 0 || (n > 0 && (!w || !wp || !eta || !m1 || !m2 || !lscale)))
+        return fail(BNSN_ERR_ARG, "invalid argument");
+    DeviceState* st;
+    int rc = device_state(&st);
+    if (rc)
+        return rc;
+    cudaError_t e = launch_nes_m(w, wp, eta, m1, m2, lscale, n, (cudaStream_t)stream,
+                                 st->num_sms);
+    return e == cudaSuccess ? BNSN_OK : cuda_fail(e, "NES integral kernel launch");
+}
+
 extern "C" int bnsn_fdi_host(int twice_order, const double* x, double* out, int64_t n)
 {
     g_err.clear();

@@ -41,6 +41,7 @@
 #include "bnsn_fp32.cuh"
 #include "bnsn_mixed.cuh"
 #include "bnsn_fp64.cuh"
+#include "bnsn_nes32.cuh"
 #include "bnsn_pair32.cuh"
 #include "bnsn_internal.h"
 
@@ -1313,6 +1314,73 @@ __device__ __forceinline__ void neps_item_mixed(const NepsPoint& P, const NepsMi
     }
 }
 
+// One item of the mixed fast pass: r1 = R(nu, nub) / pre per species, summed
+// over e- and e+, from the cancellation-free FP32 integrals of
+// bnsn_nes32.cuh (R(nub, nu) = -R(nu, nub) needs no second integral), with
+// NEPSExpFunc applied as in neps_item_mixed.  The Taylor branches of
+// kernel_nes.hpp:82-132 (w or w' below 1e-3 eta) stay FP64, as there.
+__device__ __forceinline__ void neps_item_q(const NepsPoint& P, double w, double wp,
+                                            float* em1, float* ab1, float* em2, float* ab2)
+{
+    const double x = (w > wp) ? w : wp;
+    const double y = (w < wp) ? w : wp;
+    const double d1 = wp - w, d2 = w - wp;
+    const bool n1 = signbit(d1) != 0, n2 = signbit(d2) != 0;
+    const float efa = neps_exp_f32(d1, n1);
+    const float efb = neps_exp_f32(d2, n2);
+    const float sign1 = n1 ? 1.f : -1.f;
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+        em1[s] = ab1[s] = em2[s] = ab2[s] = 0.f;
+    const nes32::Geo G = nes32::make_geo(w, wp);
+    const float ixy = (float)(1. / ((x * y) * (x * y)));
+    // e+ terms scale as e^{-eta_e}: below 1e-13 of the e- terms for eta_e > 30
+    const int nlep = P.eta0 > 30. ? 1 : 2;
+#pragma unroll 1
+    for (int e = 0; e < nlep; ++e)
+    {
+        const double eta = e ? P.eta1 : P.eta0;
+        float r1[4], r2[4];
+        if (y > eta * 1e-3)
+        {
+            float I1, I2;
+            double lref;
+            nes32::lepton_integrals(G, eta, I1, I2, lref);
+            const float sc = sign1 * ixy * expf((float)lref);
+            const float A = I1 * sc, B = I2 * sc; // the b1 and b2 parts of R
+            constexpr float kBp = (float)k::NepsBPlus, kBm = (float)k::NepsBMinus,
+                            kBz = (float)k::NepsBZero;
+#pragma unroll
+            for (int s = 0; s < 4; ++s)
+            {
+                const float bo   = (s < 2) ? kBp : kBm;
+                const bool first = ((s & 1) == 0) != (e == 1); // b1 = bo, b2 = B0
+                r1[s] = first ? fmaf(A, bo, B * kBz) : fmaf(A, kBz, B * bo);
+                r2[s] = -r1[s];
+            }
+        }
+        else
+        {
+            double t1[4], t2[4];
+            neps_taylor(P, e, w, wp, x, y, (int)sign1, n1 ? -1 : 1, t1, t2);
+#pragma unroll
+            for (int s = 0; s < 4; ++s)
+            {
+                r1[s] = (float)t1[s];
+                r2[s] = (float)t2[s];
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < 4; ++s)
+        {
+            em1[s] += -r1[s] * efb;
+            ab1[s] += r1[s] * efa;
+            em2[s] += -r2[s] * efa;
+            ab2[s] += r2[s] * efb;
+        }
+    }
+}
+
 // MIXED: double-float items, FP64 points flagged for the second launch.
 // !MIXED: FP64 items (all points, or with FP64_ONLY_FLAGGED only the points the
 // mixed launch flagged).
@@ -1581,7 +1649,7 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
                     if (MODE == kNesFast)
                     {
                         float em1[4], ab1[4], em2[4], ab2[4];
-                        neps_item_mixed(NP, Q, &s_ftab, w, wp, em1, ab1, em2, ab2);
+                        neps_item_q(NP, w, wp, em1, ab1, em2, ab2);
                         float g[4], gm[4], gb[4], gbm[4];
                         total_nu_f32(nu, lnu, Q, g, gm);
                         total_nu_f32(nub, lnub, Q, gb, gbm);
@@ -1912,7 +1980,43 @@ __global__ void __launch_bounds__(128)
     }
 }
 
+// The mixed path's NES/NPS out-kernel integrals at given (w, w', eta):
+// MezzacappaIntOut(w, w', b1, b2) of kernel_nes.hpp:50-78 (the general
+// branch, without the Taylor expansions) = e^{ls} (b1 m1 + b2 m2).
+__global__ void __launch_bounds__(128)
+    nes_m_kernel(const double* __restrict__ w, const double* __restrict__ wp,
+                 const double* __restrict__ eta, double* __restrict__ m1,
+                 double* __restrict__ m2, double* __restrict__ ls, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+    {
+        const nes32::Geo G = nes32::make_geo(w[i], wp[i]);
+        float I1, I2;
+        double lref;
+        nes32::lepton_integrals(G, eta[i], I1, I2, lref);
+        const double xy  = w[i] * wp[i];
+        const double sgn = w[i] > wp[i] ? 1. : -1.;
+        m1[i] = sgn * (double)I1 / (xy * xy);
+        m2[i] = sgn * (double)I2 / (xy * xy);
+        ls[i] = lref;
+    }
+}
+
 } // namespace
+
+cudaError_t launch_nes_m(const double* w, const double* wp, const double* eta, double* m1,
+                         double* m2, double* ls, int64_t n, cudaStream_t st, int sms)
+{
+    if (n <= 0)
+        return cudaSuccess;
+    const int64_t blocks = (n + 127) / 128;
+    const int grid       = (int)(blocks < (int64_t)sms * 8 ? blocks : (int64_t)sms * 8);
+    phase_mark(kPhAux, 0, st);
+    nes_m_kernel<<<grid, 128, 0, st>>>(w, wp, eta, m1, m2, ls, n);
+    phase_mark(kPhAux, 1, st);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_pair_j(const double* y, const double* z, const double* eta, double* j0,
                           double* j1, double* ls, int64_t n, cudaStream_t st, int sms)

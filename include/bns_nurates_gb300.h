@@ -466,6 +466,17 @@ int bnsn_fdi_host(int twice_order, const double* x, double* out, int64_t n);
 int bnsn_pair_j_mixed(const double* y, const double* z, const double* eta, double* j0,
                       double* j1, double* lscale, int64_t n, void* stream);
 
+/* The mixed path's NES/NPS out-kernel integrals at n given (w, w', eta),
+ * device arrays, stream-ordered: MezzacappaIntOut(w, w', b1, b2) of
+ * kernel_nes.hpp:50-78 (w = omega/T, w' = omega'/T, eta = mu/T of the lepton;
+ * the general branch, not the reference's Taylor expansions for small
+ * energies) = exp(lscale) * (b1 m1 + b2 m2).  The mixed grey path computes it
+ * as a positive FP32 integral over the lepton energy instead of the
+ * reference's cancelling Fermi-integral combination; this entry exposes that
+ * integral for testing. */
+int bnsn_nes_m_mixed(const double* w, const double* wp, const double* eta, double* m1,
+                     double* m2, double* lscale, int64_t n, void* stream);
+
 /* Gauss-Legendre nodes/weights of order quad->nx on [0,1]; replaces
  * GaussLegendre (integration.hpp:28-87), same algorithm. */
 int bnsn_gauss_legendre(MyQuadrature* quad);
