@@ -44,6 +44,7 @@ struct OpacityLaunch
     double lx2[kMaxQ], l1m[kMaxQ], l1p[kMaxQ]; // NES: log x_i, log(1 - x_i), log(1 + x_i)
     double lx1[kMaxQ];     // spectral: log of the 1-D nodes
     uint32_t cells[kMaxCells]; // a | b << 16, a <= b
+    uint16_t nes_order[2 * kMaxQ * kMaxQ]; // NES items (r, i, j) by ascending max(w, w')
     Gp19Dev gp19;
     // spectral launches only
     int n_energies;        // energies of this launch (<= 64)

@@ -49,32 +49,8 @@ struct NepsMixed
 {
     dfm::df reta[2][5]; // unreflected F_1..F_5 at eta for e- (0) and e+ (1)
     dfm::df eta[2];
-    float wt[4], wf[4];
     double invTt[4], etat[4], lbf[4], invTf[4], cf[4]; // exponent arguments in FP64
 };
-
-// TotalNuF (distribution.hpp:298-315) and 1 - TotalNuF in FP32 with the
-// exponent arguments formed in FP64 (they cancel: omega/T_t - eta_t, and
-// log beta_f + c_f log omega - omega/T_f); lw = log omega.  The blocking
-// factor is formed from the complements of the two parts (w_t + w_f = 1 for
-// the reconstructed distribution), so it keeps its relative precision where
-// the occupation approaches 1.
-__device__ __forceinline__ void total_nu_f32(double omega, double lw, const NepsMixed& Q, float* g,
-                                             float* gm)
-{
-#pragma unroll
-    for (int s = 0; s < 4; ++s)
-    {
-        const float arg = (float)fma(omega, Q.invTt[s], -Q.etat[s]);
-        const float t   = expf(-fabsf(arg));
-        const float inv = 1.f / (t + 1.f);
-        const float ft  = arg > 0.f ? t * inv : inv;
-        const float ftm = arg > 0.f ? inv : t * inv;
-        const float fn  = expf((float)fma(Q.cf[s], lw, fma(-omega, Q.invTf[s], Q.lbf[s])));
-        g[s]            = Q.wt[s] * ft + Q.wf[s] * fn;
-        gm[s]           = Q.wt[s] * ftm + Q.wf[s] * (1.f - fn);
-    }
-}
 
 // NEPSExpFunc (functions.hpp:4401-4413) in FP32 for the FP64 argument d;
 // e^{-|d|} takes the FP32 exponential of the rounded argument times the

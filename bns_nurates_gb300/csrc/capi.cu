@@ -212,6 +212,23 @@ int fill_common(const MyQuadrature* q1, const MyQuadrature* q2, const OpacityFla
     L->ncell = (int)cells.size();
     for (int c = 0; c < L->ncell; ++c)
         L->cells[c] = cells[c].second;
+    // NES items r * n2^2 + i * n2 + j by ascending max(w, w'): the quadrature
+    // cost of an item grows with its extent, and a warp's lanes take
+    // consecutive items
+    std::vector<std::pair<double, uint16_t>> items;
+    items.reserve(2 * n2 * n2);
+    for (int r = 0; r < 2; ++r)
+        for (int i = 0; i < n2; ++i)
+            for (int j = 0; j < n2; ++j)
+            {
+                const double xi = q2->points[i], xj = q2->points[j];
+                const double x  = r ? (1. + xj) / xi : xi * (1. + xj);
+                items.push_back({x, (uint16_t)((r * n2 + i) * n2 + j)});
+            }
+    std::stable_sort(items.begin(), items.end(),
+                     [](const auto& u, const auto& v) { return u.first < v.first; });
+    for (size_t c = 0; c < items.size(); ++c)
+        L->nes_order[c] = items[c].second;
     return BNSN_OK;
 }
 

@@ -1210,180 +1210,6 @@ __device__ __forceinline__ void neps_items_fp64(const NepsPoint& NP, const Distr
     }
 }
 
-// One item of the mixed path: dimensionless kernels r1 = R(nu, nub) / pre,
-// r2 = R(nub, nu) / pre summed over e- and e+ with NEPSExpFunc applied
-// (em1, ab1, em2, ab2 per species).  The Fermi integrals and the
-// Mezzacappa-Bruenn brackets (kernel_nes.hpp:50-132) run in df: they cancel
-// catastrophically.  The branch structure of neps_pair is kept; the Taylor
-// branches near w, w' -> 0 run in FP64.
-__device__ __forceinline__ void neps_item_mixed(const NepsPoint& P, const NepsMixed& Q,
-                                                const dfm::FdiTab* ftab, double w, double wp,
-                                                float* em1, float* ab1, float* em2, float* ab2)
-{
-    using namespace dfm;
-    const double x = (w > wp) ? w : wp;
-    const double y = (w < wp) ? w : wp;
-    const double d1 = wp - w, d2 = w - wp;
-    const bool n1 = signbit(d1) != 0, n2 = signbit(d2) != 0;
-    const float efa = neps_exp_f32(d1, n1);
-    const float efb = neps_exp_f32(d2, n2);
-    const float sign1 = n1 ? 1.f : -1.f;
-    const float sign2 = n2 ? 1.f : -1.f;
-#pragma unroll
-    for (int s = 0; s < 4; ++s)
-        em1[s] = ab1[s] = em2[s] = ab2[s] = 0.f;
-    // w-dependent df building blocks shared by both leptons
-    const df W  = from_double(w), WP = from_double(wp);
-    const df S  = add(W, WP);
-    const df Pp = mul(W, WP);
-    const df Dn = mul(Pp, Pp);
-    const df iDn = div(mk(1.f), Dn); // the four brackets per lepton share 1 / Dn
-    const df X  = from_double(x), Y = from_double(y);
-    // e+ terms scale as e^{-eta_e}: below 1e-13 of the e- terms for eta_e > 30
-    const int nlep = P.eta0 > 30. ? 1 : 2;
-#pragma unroll 1
-    for (int e = 0; e < nlep; ++e)
-    {
-        const double eta = e ? P.eta1 : P.eta0;
-        float r1[4], r2[4];
-        if (y > eta * 1e-3)
-        {
-            // F_k(eta - w'), F_k(eta - w) and F_k(eta) - F_k(eta - |w - w'|) as
-            // differences (fdi_diff15): no cancellation of the reflection
-            // polynomials in degenerate matter
-            const df aw = from_double(eta - w), awp = from_double(eta - wp);
-            const double adw = fabs(w - wp);
-            const df aab = from_double(eta - adw);
-            df rw[5], rwp[5], rab[5];
-            fdi_raw15(aw, rw, 1, ftab);
-            fdi_raw15(awp, rwp, 1, ftab);
-            fdi_raw15(aab, rab, 3, ftab); // only F_3..F_5 enter through |w - w'|
-            rab[0] = rab[1] = Q.reta[e][0]; // unused orders: keep the arrays defined
-            df dw[5], d5[5];
-            fdi_diff15(rw, rwp, aw, awp, from_double(w - wp), dw);
-            fdi_diff15(rab, Q.reta[e], aab, Q.eta[e], from_double(adw), d5);
-            const df dabs[3] = {d5[2], d5[3], d5[4]};
-            // mb_int_out(w, w') = b1 A + b2 B; the (w', w) direction has
-            // dw -> -dw and the other sign (kernel_nes.hpp:50-78)
-            const df T1 = add(dw[3], mul(add(mul(S, dw[2]), mul(mul(Pp, 3.f), dw[1])), 2.f));
-            const df U  = add(mul(X, dabs[1]), mul(mul(mul(X, X), 2.f), dabs[0]));
-            const df V  = add(neg(mul(Y, dabs[1])), mul(mul(mul(Y, Y), 2.f), dabs[0]));
-            const df ST = mul(S, T1);
-            constexpr dfc kFifth(0.2); // 0.2f is not 0.2: the brackets cancel to 1e-6
-            const df d2 = mul(dabs[2], mk(kFifth)), w4 = mul(dw[4], mk(kFifth));
-            const df c1 = sub(mul(d2, sign1), w4);
-            const df c2 = add(mul(d2, sign2), w4);
-            const df s6 = mul(dw[0], 6.f);
-            const df A1 = sub(mul(add(sub(c1, ST), mul(U, sign1)), iDn), s6);
-            const df B1 = mul(add(c1, mul(V, sign1)), iDn);
-            const df A2 = add(mul(add(add(c2, ST), mul(U, sign2)), iDn), s6);
-            const df B2 = mul(add(c2, mul(V, sign2)), iDn);
-            // couplings of neps_couplings: species s pairs (b1, b2) from
-            // {B+ or B-, B0} in an order set by the lepton
-            constexpr dfc kBp(k::NepsBPlus), kBm(k::NepsBMinus), kBz(k::NepsBZero);
-            const df Az1 = mul(A1, mk(kBz)), Bz1 = mul(B1, mk(kBz));
-            const df Az2 = mul(A2, mk(kBz)), Bz2 = mul(B2, mk(kBz));
-#pragma unroll
-            for (int s = 0; s < 4; ++s)
-            {
-                const df bo     = (s < 2) ? mk(kBp) : mk(kBm);
-                const bool first = ((s & 1) == 0) != (e == 1); // b1 = bo, b2 = B0
-                r1[s] = first ? add(mul(A1, bo), Bz1).hi : add(Az1, mul(B1, bo)).hi;
-                r2[s] = first ? add(mul(A2, bo), Bz2).hi : add(Az2, mul(B2, bo)).hi;
-            }
-        }
-        else
-        {
-            double t1[4], t2[4];
-            neps_taylor(P, e, w, wp, x, y, (int)sign1, (int)sign2, t1, t2);
-#pragma unroll
-            for (int s = 0; s < 4; ++s)
-            {
-                r1[s] = (float)t1[s];
-                r2[s] = (float)t2[s];
-            }
-        }
-#pragma unroll
-        for (int s = 0; s < 4; ++s)
-        {
-            em1[s] += -r1[s] * efb;
-            ab1[s] += r1[s] * efa;
-            em2[s] += -r2[s] * efa;
-            ab2[s] += r2[s] * efb;
-        }
-    }
-}
-
-// One item of the mixed fast pass: r1 = R(nu, nub) / pre per species, summed
-// over e- and e+, from the cancellation-free FP32 integrals of
-// bnsn_nes32.cuh (R(nub, nu) = -R(nu, nub) needs no second integral), with
-// NEPSExpFunc applied as in neps_item_mixed.  The Taylor branches of
-// kernel_nes.hpp:82-132 (w or w' below 1e-3 eta) stay FP64, as there.
-__device__ __forceinline__ void neps_item_q(const NepsPoint& P, double w, double wp,
-                                            float* em1, float* ab1, float* em2, float* ab2)
-{
-    const double x = (w > wp) ? w : wp;
-    const double y = (w < wp) ? w : wp;
-    const double d1 = wp - w, d2 = w - wp;
-    const bool n1 = signbit(d1) != 0, n2 = signbit(d2) != 0;
-    const float efa = neps_exp_f32(d1, n1);
-    const float efb = neps_exp_f32(d2, n2);
-    const float sign1 = n1 ? 1.f : -1.f;
-#pragma unroll
-    for (int s = 0; s < 4; ++s)
-        em1[s] = ab1[s] = em2[s] = ab2[s] = 0.f;
-    const nes32::Geo G = nes32::make_geo(w, wp);
-    const float ixy = (float)(1. / ((x * y) * (x * y)));
-    // e+ terms scale as e^{-eta_e}: below 1e-13 of the e- terms for eta_e > 30
-    const int nlep = P.eta0 > 30. ? 1 : 2;
-#pragma unroll 1
-    for (int e = 0; e < nlep; ++e)
-    {
-        const double eta = e ? P.eta1 : P.eta0;
-        float r1[4], r2[4];
-        if (y > eta * 1e-3)
-        {
-            float I1, I2;
-            double lref;
-            nes32::lepton_integrals(G, eta, I1, I2, lref);
-            const float sc = sign1 * ixy * expf((float)lref);
-            const float A = I1 * sc, B = I2 * sc; // the b1 and b2 parts of R
-            constexpr float kBp = (float)k::NepsBPlus, kBm = (float)k::NepsBMinus,
-                            kBz = (float)k::NepsBZero;
-#pragma unroll
-            for (int s = 0; s < 4; ++s)
-            {
-                const float bo   = (s < 2) ? kBp : kBm;
-                const bool first = ((s & 1) == 0) != (e == 1); // b1 = bo, b2 = B0
-                r1[s] = first ? fmaf(A, bo, B * kBz) : fmaf(A, kBz, B * bo);
-                r2[s] = -r1[s];
-            }
-        }
-        else
-        {
-            double t1[4], t2[4];
-            neps_taylor(P, e, w, wp, x, y, (int)sign1, n1 ? -1 : 1, t1, t2);
-#pragma unroll
-            for (int s = 0; s < 4; ++s)
-            {
-                r1[s] = (float)t1[s];
-                r2[s] = (float)t2[s];
-            }
-        }
-#pragma unroll
-        for (int s = 0; s < 4; ++s)
-        {
-            em1[s] += -r1[s] * efb;
-            ab1[s] += r1[s] * efa;
-            em2[s] += -r2[s] * efa;
-            ab2[s] += r2[s] * efb;
-        }
-    }
-}
-
-// MIXED: double-float items, FP64 points flagged for the second launch.
-// !MIXED: FP64 items (all points, or with FP64_ONLY_FLAGGED only the points the
-// mixed launch flagged).
 // TotalNuF and 1 - TotalNuF in df (the accurate pass of the mixed path).
 __device__ __forceinline__ void total_nu_df(double omega, double lw, const NepsMixed& Q,
                                             const double* wt, const double* wf, dfm::df* g,
@@ -1506,26 +1332,26 @@ __device__ __forceinline__ void neps_item_df(const NepsPoint& P, const NepsMixed
 
 // NES launch modes.  The plain path runs kNesFp64All.  The mixed path runs
 // three launches per chunk, each over all points but working only on its own:
-//   kNesFast      double-float Fermi integrals, FP32 weights; flags a point 1
-//                 when its sums cancel (terms of both signs, or negative pair +
-//                 brem sums) and 2 when it leaves the FP32/df range envelope;
+//   grey_nes_fast_kernel  FP32 kernel integrals (bnsn_nes32.cuh); flags a
+//                 point 1 when its sums cancel (terms of both signs, or
+//                 negative pair + brem sums) and 2 when it leaves the FP32
+//                 range envelope;
 //   kNesAccurate  flag 1: every product in df (cancellation up to ~1e5);
 //                 beyond that the point is flagged 2;
 //   kNesFp64Flag  flag 2: FP64 items.
 enum NesMode
 {
     kNesFp64All = 0,
-    kNesFast,
-    kNesAccurate,
+    kNesAccurate = 2,
     kNesFp64Flag
 };
 
 template <int MODE>
-__global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNesAccurate) ? 4 : 1)
+__global__ void __launch_bounds__(kWarps * 32, MODE == kNesAccurate ? 4 : 1)
     grey_neps_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
                      double* __restrict__ scratch)
 {
-    constexpr bool MIX = MODE == kNesFast || MODE == kNesAccurate;
+    constexpr bool MIX = MODE == kNesAccurate;
     __shared__ double s_x2[kMaxQ], s_w2[kMaxQ], s_wx[kMaxQ], s_wx3[kMaxQ];
     __shared__ NepsTab s_nt[kWarps];
     __shared__ NepsMixed s_nm[MIX ? kWarps : 1];
@@ -1585,23 +1411,6 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
         else
         {
             int flag = 0;
-            if (MODE == kNesFast)
-            {
-                // range envelope: the occupation of every species must stay far
-                // above the FP32 normal range at its peak
-                bool ok = isfinite(NP.eta0);
-#pragma unroll
-                for (int s = 0; s < 4; ++s)
-                {
-                    const Distr& d = N.d;
-                    ok = ok && (d.w_t[s] == 0. || d.eta_t[s] > -60.) &&
-                         (d.w_f[s] == 0. || d.beta_f[s] > 1e-30) && (d.temp_t[s] > 0.) &&
-                         (d.temp_f[s] > 0.) && isfinite(d.eta_t[s]) && isfinite(d.beta_f[s]);
-                }
-                if (!ok)
-                    flag = 2;
-            }
-            if (flag == 0)
             {
                 NepsMixed& Q = s_nm[MIX ? wid : 0];
                 if (lane < 2)
@@ -1613,10 +1422,8 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
                 {
                     const int s    = lane - 8;
                     const Distr& d = N.d;
-                    Q.wt[s]    = (float)d.w_t[s];
                     Q.invTt[s] = 1. / d.temp_t[s];
                     Q.etat[s]  = d.eta_t[s];
-                    Q.wf[s]    = (float)d.w_f[s];
                     Q.lbf[s]   = d.beta_f[s] > 0. ? log(d.beta_f[s]) : -INFINITY;
                     Q.invTf[s] = 1. / d.temp_f[s];
                     Q.cf[s]    = d.c_f[s];
@@ -1646,52 +1453,6 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
                     const double lnu  = lhtn + (r ? lm - lx : lx + lm);
                     const double lnub = lhtn + (r ? lp - lx : lx + lp);
                     const double Wr   = (r ? s_wx3[i] : s_wx[i]) * s_w2[j];
-                    if (MODE == kNesFast)
-                    {
-                        float em1[4], ab1[4], em2[4], ab2[4];
-                        neps_item_q(NP, w, wp, em1, ab1, em2, ab2);
-                        float g[4], gm[4], gb[4], gbm[4];
-                        total_nu_f32(nu, lnu, Q, g, gm);
-                        total_nu_f32(nub, lnub, Q, gb, gbm);
-                        const float fw = (float)w, fwp = (float)wp;
-                        const float w4 = (fw * fwp) * (fw * fwp);
-                        const float Wf = (float)Wr;
-#pragma unroll
-                        for (int s = 0; s < 4; ++s)
-                        {
-                            const float e1 = em1[s] * gb[s];
-                            const float a1 = ab1[s] * (nbb ? 1.f : gbm[s]);
-                            const float e2 = em2[s] * g[s];
-                            const float a2 = ab2[s] * (nbb ? 1.f : gm[s]);
-                            float EM1, AB1, EM2, AB2;
-                            if (L.stim)
-                            {
-                                AB1 = w4 * g[s] * (e1 + a1);
-                                EM1 = w4 * e1;
-                                AB2 = w4 * gb[s] * (e2 + a2);
-                                EM2 = w4 * e2;
-                            }
-                            else
-                            {
-                                AB1 = w4 * g[s] * a1;
-                                EM1 = w4 * gm[s] * e1;
-                                AB2 = w4 * gb[s] * a2;
-                                EM2 = w4 * gbm[s] * e2;
-                            }
-                            const float tem = Wf * (EM1 + EM2), tab = Wf * (AB1 + AB2);
-                            const float tee = Wf * (fw * EM1 + fwp * EM2);
-                            const float tae = Wf * (fw * AB1 + fwp * AB2);
-                            dacc[s]      = dfm::add(dacc[s], tem);
-                            dacc[4 + s]  = dfm::add(dacc[4 + s], tab);
-                            dacc[8 + s]  = dfm::add(dacc[8 + s], tee);
-                            dacc[12 + s] = dfm::add(dacc[12 + s], tae);
-                            mag[s] += fabsf(tem);
-                            mag[4 + s] += fabsf(tab);
-                            mag[8 + s] += fabsf(tee);
-                            mag[12 + s] += fabsf(tae);
-                        }
-                    }
-                    else
                     {
                         using namespace dfm;
                         df em1[4], ab1[4], em2[4], ab2[4];
@@ -1762,13 +1523,13 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
                                      ? 0.125 * P->s2d[kk] * (kk >= 8 ? t2d : 1.)
                                      : 0.;
                 const double amp = cancel_factor(acc, mag, NP.pre * T4, NP.pre * T4 * T, other);
-                if (amp > (MODE == kNesFast ? kMaxCancel : kMaxCancelDf))
-                    flag = MODE == kNesFast ? 1 : 2;
+                if (amp > kMaxCancelDf)
+                    flag = 2;
 #pragma unroll
                 for (int kk = 0; kk < 16; ++kk)
                     acc[kk] *= NP.pre * T4 * (kk >= 8 ? T : 1.);
             }
-            if (MODE == kNesFast || flag != 0)
+            if (flag != 0)
             {
                 if (lane == 0)
                     P->neps_fp64 = (double)flag;
@@ -1776,6 +1537,408 @@ __global__ void __launch_bounds__(kWarps * 32, (MODE == kNesFast || MODE == kNes
             if (flag != 0)
                 continue; // a later launch writes this point's sums
         }
+#pragma unroll
+        for (int kk = 0; kk < 16; ++kk)
+            acc[kk] = warp_sum(acc[kk]);
+        if (lane == 0)
+        {
+#pragma unroll
+            for (int kk = 0; kk < 16; ++kk)
+                P->snes[kk] = acc[kk];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// NES/NPS fast pass of the mixed path (InelasticScattKernels and the grey
+// item sums of m1_opacities.hpp:880-905): one warp per point, one item per
+// lane, the kernel integrals of bnsn_nes32.cuh in FP32.
+// ---------------------------------------------------------------------------
+
+constexpr int kNesWarps = 8;
+constexpr int kNesItems = 2 * kMaxQ * kMaxQ;
+
+// One (w, w') item.  w = nu/T and w' = nubar/T depend only on the quadrature
+// nodes, so one table per CTA serves every point; the table follows the
+// host's item order (ascending max(w, w')), which keeps a warp's lanes on
+// items of similar quadrature cost.
+struct NesItem
+{
+    float wh, wl, wph, wpl;     // w, w' as df
+    float lwh, lwl, lwph, lwpl; // log w, log w' as df
+    float sefa, sefb;           // sign x NEPSExpFunc(w' - w), sign x NEPSExpFunc(w - w')
+    float wf;                   // quadrature weight
+    float pad;
+};
+
+// TotalNuF of one species with its exponent arguments in df form:
+// w rt - eta_t and P0 + c_f log w - w rf, rt = T/T_t, rf = T/T_f,
+// P0 = log beta_f + c_f log T (distribution.hpp:298-315).
+struct NuSpecies
+{
+    dfm::df etat, rt, P0, cf, rf;
+    float wt, wf;
+};
+
+// Per-warp data of the point in work.
+struct NesWarp
+{
+    NepsTab N; // distribution and F_k(eta) for the FP64 Taylor branches
+    nes32::Lepton lep[2];
+    NuSpecies sp[4];
+};
+
+struct NesSmem
+{
+    NesItem items[kNesItems];
+    NesWarp w[kNesWarps];
+    uint16_t q[kNesWarps][kNesItems]; // items (| lepton mask << 14) for the Taylor branches
+    float2 dacc[16][kNesWarps * 32];  // per-lane df sums of the 16 moments
+    float4 mag[4][kNesWarps * 32];    // per-lane sums of |term|
+};
+
+__device__ __forceinline__ void total_nu_q(dfm::df W, dfm::df LW, const NuSpecies* sp, float* g,
+                                           float* gm)
+{
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+    {
+        const NuSpecies& S = sp[s];
+        // the product's leading part and eta_t cancel inside one FMA
+        const float a =
+            fmaf(W.hi, S.rt.hi, -S.etat.hi) + fmaf(W.hi, S.rt.lo, fmaf(W.lo, S.rt.hi, -S.etat.lo));
+        const float t   = expf(-fabsf(a));
+        const float inv = nes32::rcp_nr(t + 1.f);
+        const float ft  = a > 0.f ? t * inv : inv;
+        const float ftm = a > 0.f ? inv : t * inv;
+        float fn        = 0.f;
+        if (S.wf != 0.f)
+        {
+            const dfm::df p1 = dfm::two_prod(S.cf.hi, LW.hi);
+            const dfm::df p2 = dfm::two_prod(-W.hi, S.rf.hi);
+            const dfm::df s1 = dfm::two_sum(S.P0.hi, p1.hi);
+            const dfm::df s2 = dfm::two_sum(s1.hi, p2.hi);
+            const float lo   = (S.P0.lo + p1.lo + p2.lo + s1.lo + s2.lo) +
+                             fmaf(S.cf.hi, LW.lo, S.cf.lo * LW.hi) -
+                             fmaf(W.hi, S.rf.lo, W.lo * S.rf.hi);
+            fn = expf(s2.hi + lo);
+        }
+        g[s]  = S.wt * ft + S.wf * fn;
+        gm[s] = S.wt * ftm + S.wf * (1.f - fn);
+    }
+}
+
+// Adds one item's terms to the lane's sums: em1..ab2 are R(nu, nubar) and
+// R(nubar, nu) with NEPSExpFunc applied, times (w w')^2 (m1_opacities.hpp:880-905).
+__device__ __forceinline__ void nes_accumulate(NesSmem& S, int t, bool stim, bool nbb, float Wf,
+                                               float fw, float fwp, const float* g,
+                                               const float* gm, const float* gb,
+                                               const float* gbm, const float* em1,
+                                               const float* ab1, const float* em2,
+                                               const float* ab2)
+{
+    float tm[16];
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+    {
+        const float e1 = em1[s] * gb[s];
+        const float a1 = ab1[s] * (nbb ? 1.f : gbm[s]);
+        const float e2 = em2[s] * g[s];
+        const float a2 = ab2[s] * (nbb ? 1.f : gm[s]);
+        float EM1, AB1, EM2, AB2;
+        if (stim)
+        {
+            AB1 = g[s] * (e1 + a1);
+            EM1 = e1;
+            AB2 = gb[s] * (e2 + a2);
+            EM2 = e2;
+        }
+        else
+        {
+            AB1 = g[s] * a1;
+            EM1 = gm[s] * e1;
+            AB2 = gb[s] * a2;
+            EM2 = gbm[s] * e2;
+        }
+        tm[s]      = Wf * (EM1 + EM2);
+        tm[4 + s]  = Wf * (AB1 + AB2);
+        tm[8 + s]  = Wf * (fw * EM1 + fwp * EM2);
+        tm[12 + s] = Wf * (fw * AB1 + fwp * AB2);
+    }
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk)
+    {
+        const float2 a   = S.dacc[kk][t];
+        const dfm::df r  = dfm::add(dfm::df{a.x, a.y}, tm[kk]);
+        S.dacc[kk][t]    = make_float2(r.hi, r.lo);
+    }
+#pragma unroll
+    for (int k4 = 0; k4 < 4; ++k4)
+    {
+        float4 m = S.mag[k4][t];
+        m.x += fabsf(tm[4 * k4]);
+        m.y += fabsf(tm[4 * k4 + 1]);
+        m.z += fabsf(tm[4 * k4 + 2]);
+        m.w += fabsf(tm[4 * k4 + 3]);
+        S.mag[k4][t] = m;
+    }
+}
+
+__global__ void __launch_bounds__(kNesWarps * 32, 2)
+    grey_nes_fast_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
+                         double* __restrict__ scratch)
+{
+    extern __shared__ __align__(16) unsigned char nes_smem_raw[];
+    NesSmem& S   = *reinterpret_cast<NesSmem*>(nes_smem_raw);
+    const int n2 = L.n2, nn2 = n2 * n2, nit = 2 * nn2;
+    {
+        // w = c x_i (1 -+ x_j) for r = 0 and c (1 -+ x_j) / x_i for r = 1, c = 2 x 2.182
+        constexpr double c = 2. * k::TempMultiple;
+        const double lc    = log(c);
+        for (int k = threadIdx.x; k < nit; k += blockDim.x)
+        {
+            const int it    = L.nes_order[k];
+            const int r     = it >= nn2;
+            const int rem   = it - r * nn2;
+            const int i     = rem / n2, j = rem - (rem / n2) * n2;
+            const double xi = L.x2[i], xj = L.x2[j];
+            const double w  = r ? c * (1. - xj) / xi : c * xi * (1. - xj);
+            const double wp = r ? c * (1. + xj) / xi : c * xi * (1. + xj);
+            const double lw  = lc + (r ? L.l1m[j] - L.lx2[i] : L.lx2[i] + L.l1m[j]);
+            const double lwp = lc + (r ? L.l1p[j] - L.lx2[i] : L.lx2[i] + L.l1p[j]);
+            const double d1 = wp - w, d2 = w - wp;
+            const bool n1 = signbit(d1) != 0, n2b = signbit(d2) != 0;
+            const float sg = n1 ? 1.f : -1.f; // the reference's sign of R(w, w')
+            NesItem I;
+            dfm::df t = dfm::from_double(w);
+            I.wh = t.hi, I.wl = t.lo;
+            t = dfm::from_double(wp);
+            I.wph = t.hi, I.wpl = t.lo;
+            t = dfm::from_double(lw);
+            I.lwh = t.hi, I.lwl = t.lo;
+            t = dfm::from_double(lwp);
+            I.lwph = t.hi, I.lwpl = t.lo;
+            I.sefa = sg * neps_exp_f32(d1, n1);
+            I.sefb = sg * neps_exp_f32(d2, n2b);
+            I.wf   = (float)((r ? L.wx3[i] : L.wx[i]) * L.w2[j]);
+            I.pad  = 0.f;
+            S.items[k] = I;
+        }
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int wid  = threadIdx.x >> 5;
+    const int t    = threadIdx.x;
+    NesWarp& Wd    = S.w[wid];
+    uint16_t* qw   = S.q[wid];
+    const bool nbb  = L.neglect_blocking != 0;
+    const bool stim = L.stim != 0;
+    const int64_t nwarp = (int64_t)gridDim.x * kNesWarps;
+    constexpr float kBp = (float)k::NepsBPlus, kBm = (float)k::NepsBMinus,
+                    kBz = (float)k::NepsBZero;
+
+    for (int64_t qp = (int64_t)blockIdx.x * kNesWarps + wid; qp < np; qp += nwarp)
+    {
+        const int64_t p = L.pidx ? L.pidx[p0 + qp] : p0 + qp;
+        PointTab* P     = (PointTab*)(scratch + qp * kTabWords);
+        const double T = L.eos[1][p], mu_e = L.eos[7][p];
+        __syncwarp();
+        warp_copy((double*)&Wd.N.d, (const double*)&P->d, 28 + 12 + 2, lane);
+        if (lane == 0)
+            Wd.N.same_cf = P->same_cf;
+        __syncwarp();
+        NepsPoint NP;
+        NP.T    = T;
+        NP.pre  = k::NepsConst * (T * T);
+        NP.eta0 = mu_e / T;
+        NP.eta1 = -mu_e / T;
+        NP.fd00 = Wd.N.fd0[0];
+        NP.fd01 = Wd.N.fd0[1];
+        NP.fe0  = Wd.N.fe[0];
+        NP.fe1  = Wd.N.fe[1];
+        // range envelope: the occupation of every species far above the FP32
+        // normal range at its peak; e^{-Lref} of the e+ integrals finite
+        bool ok = isfinite(NP.eta0) && NP.eta0 > -80.;
+#pragma unroll
+        for (int s = 0; s < 4; ++s)
+        {
+            const Distr& d = Wd.N.d;
+            ok = ok && (d.w_t[s] == 0. || d.eta_t[s] > -60.) &&
+                 (d.w_f[s] == 0. || d.beta_f[s] > 1e-30) && (d.temp_t[s] > 0.) &&
+                 (d.temp_f[s] > 0.) && isfinite(d.eta_t[s]) && isfinite(d.beta_f[s]);
+        }
+        int flag = ok ? 0 : 2;
+        double acc[16];
+        if (flag == 0)
+        {
+            if (lane < 2)
+                Wd.lep[lane] = nes32::make_lepton(lane ? NP.eta1 : NP.eta0);
+            else if (lane >= 8 && lane < 12)
+            {
+                const int s    = lane - 8;
+                const Distr& d = Wd.N.d;
+                NuSpecies& Sp  = Wd.sp[s];
+                Sp.wt   = (float)d.w_t[s];
+                Sp.wf   = (float)d.w_f[s];
+                Sp.etat = dfm::from_double(d.eta_t[s]);
+                Sp.rt   = dfm::from_double(T / d.temp_t[s]);
+                const double lbf = d.beta_f[s] > 0. ? log(d.beta_f[s]) : 0.;
+                Sp.P0   = dfm::from_double(lbf + d.c_f[s] * log(T));
+                Sp.cf   = dfm::from_double(d.c_f[s]);
+                Sp.rf   = dfm::from_double(T / d.temp_f[s]);
+            }
+#pragma unroll
+            for (int kk = 0; kk < 16; ++kk)
+                S.dacc[kk][t] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int k4 = 0; k4 < 4; ++k4)
+                S.mag[k4][t] = make_float4(0.f, 0.f, 0.f, 0.f);
+            __syncwarp();
+            // e+ terms scale as e^{-eta_e}: below 1e-13 of the e- terms for eta_e > 30
+            const int nlep = NP.eta0 > 30. ? 1 : 2;
+            int nq = 0;
+            for (int base = 0; base < nit; base += 32)
+            {
+                const int k  = base + lane;
+                unsigned tmk = 0;
+                if (k < nit)
+                {
+                    const NesItem I    = S.items[k];
+                    const dfm::df W    = {I.wh, I.wl}, WP = {I.wph, I.wpl};
+                    const nes32::Geo G = nes32::make_geo(W, WP);
+                    // A e^{-Lref}-scaled kernel sum b1 I_1 + b2 I_2 per species
+                    // over the leptons: R(nu, nubar) (w w')^2 = sign x c
+                    float c[4] = {0.f, 0.f, 0.f, 0.f};
+                    bool any   = false;
+#pragma unroll 1
+                    for (int e = 0; e < nlep; ++e)
+                    {
+                        const nes32::Lepton& Lp = Wd.lep[e];
+                        if (!nes32::above_taylor(G, Lp))
+                        {
+                            tmk |= 1u << e;
+                            continue;
+                        }
+                        float I1, I2;
+                        nes32::lepton_integrals(G, Lp, I1, I2);
+                        const float A = Lp.A * I1, B = Lp.A * I2;
+#pragma unroll
+                        for (int s = 0; s < 4; ++s)
+                        {
+                            const float bo   = (s < 2) ? kBp : kBm;
+                            const bool first = ((s & 1) == 0) != (e == 1); // b1 = bo, b2 = B0
+                            c[s] += first ? fmaf(A, bo, B * kBz) : fmaf(A, kBz, B * bo);
+                        }
+                        any = true;
+                    }
+                    if (any)
+                    {
+                        // R(nubar, nu) = -R(nu, nubar)
+                        float em1[4], ab1[4], em2[4], ab2[4];
+#pragma unroll
+                        for (int s = 0; s < 4; ++s)
+                        {
+                            em1[s] = ab2[s] = -c[s] * I.sefb;
+                            ab1[s] = em2[s] = c[s] * I.sefa;
+                        }
+                        float g[4], gm[4], gb[4], gbm[4];
+                        total_nu_q(W, dfm::df{I.lwh, I.lwl}, Wd.sp, g, gm);
+                        total_nu_q(WP, dfm::df{I.lwph, I.lwpl}, Wd.sp, gb, gbm);
+                        nes_accumulate(S, t, stim, nbb, I.wf, I.wh, I.wph, g, gm, gb, gbm, em1,
+                                       ab1, em2, ab2);
+                    }
+                }
+                const unsigned tb = __ballot_sync(0xffffffffu, tmk != 0);
+                if (tmk)
+                    qw[nq + __popc(tb & ((1u << lane) - 1u))] = (uint16_t)(k | (tmk << 14));
+                nq += __popc(tb);
+            }
+            __syncwarp();
+            // items in the reference's Taylor branches (w or w' below 1e-3 eta,
+            // kernel_nes.hpp:82-132), FP64, all lanes busy
+            for (int base = 0; base < nq; base += 32)
+            {
+                const int qi = base + lane;
+                if (qi >= nq)
+                    continue;
+                const unsigned ent = qw[qi];
+                const int k        = (int)(ent & 0x3fffu);
+                const unsigned tmq = ent >> 14;
+                const NesItem I    = S.items[k];
+                const double w  = (double)I.wh + (double)I.wl;
+                const double wp = (double)I.wph + (double)I.wpl;
+                const double x = w > wp ? w : wp, y = w > wp ? wp : w;
+                const bool n1 = signbit(wp - w) != 0, n2b = signbit(w - wp) != 0;
+                const int sign1 = n1 ? 1 : -1, sign2 = n2b ? 1 : -1;
+                const float efa = (float)sign1 * I.sefa, efb = (float)sign1 * I.sefb;
+                const float w4  = (float)((w * wp) * (w * wp));
+                float em1[4], ab1[4], em2[4], ab2[4];
+#pragma unroll
+                for (int s = 0; s < 4; ++s)
+                    em1[s] = ab1[s] = em2[s] = ab2[s] = 0.f;
+#pragma unroll 1
+                for (int e = 0; e < 2; ++e)
+                {
+                    if (!((tmq >> e) & 1u))
+                        continue;
+                    double t1[4], t2[4];
+                    neps_taylor(NP, e, w, wp, x, y, sign1, sign2, t1, t2);
+#pragma unroll
+                    for (int s = 0; s < 4; ++s)
+                    {
+                        const float r1 = (float)t1[s] * w4, r2 = (float)t2[s] * w4;
+                        em1[s] += -r1 * efb;
+                        ab1[s] += r1 * efa;
+                        em2[s] += -r2 * efa;
+                        ab2[s] += r2 * efb;
+                    }
+                }
+                float g[4], gm[4], gb[4], gbm[4];
+                total_nu_q(dfm::df{I.wh, I.wl}, dfm::df{I.lwh, I.lwl}, Wd.sp, g, gm);
+                total_nu_q(dfm::df{I.wph, I.wpl}, dfm::df{I.lwph, I.lwpl}, Wd.sp, gb, gbm);
+                nes_accumulate(S, t, stim, nbb, I.wf, I.wh, I.wph, g, gm, gb, gbm, em1, ab1, em2,
+                               ab2);
+            }
+            float mag[16];
+#pragma unroll
+            for (int kk = 0; kk < 16; ++kk)
+            {
+                const float2 a = S.dacc[kk][t];
+                acc[kk]        = (double)a.x + (double)a.y;
+            }
+#pragma unroll
+            for (int k4 = 0; k4 < 4; ++k4)
+            {
+                const float4 m = S.mag[k4][t];
+                mag[4 * k4]     = m.x;
+                mag[4 * k4 + 1] = m.y;
+                mag[4 * k4 + 2] = m.z;
+                mag[4 * k4 + 3] = m.w;
+            }
+            // terms of both signs (occupation above 1), or NES sums cancelling
+            // the pair + brem sums of the same output (those enter the assembly
+            // with t2d^2 = hn / 8, times t2d for energy moments) or the beta
+            // rates: the point goes to the accurate pass
+            const double T4 = (T * T) * (T * T);
+            double other[16];
+            beta_in_sum_units(P, T, NP.eta0, L.use_abs_em, true, other);
+            const double t2d = k::TempMultiple * T;
+#pragma unroll
+            for (int kk = 0; kk < 16; ++kk)
+                other[kk] += (L.use_pair || L.use_brem)
+                                 ? 0.125 * P->s2d[kk] * (kk >= 8 ? t2d : 1.)
+                                 : 0.;
+            const double amp = cancel_factor(acc, mag, NP.pre * T4, NP.pre * T4 * T, other);
+            if (amp > kMaxCancel)
+                flag = 1;
+#pragma unroll
+            for (int kk = 0; kk < 16; ++kk)
+                acc[kk] *= NP.pre * T4 * (kk >= 8 ? T : 1.);
+        }
+        if (lane == 0)
+            P->neps_fp64 = (double)flag;
+        if (flag != 0)
+            continue; // a later launch writes this point's sums
 #pragma unroll
         for (int kk = 0; kk < 16; ++kk)
             acc[kk] = warp_sum(acc[kk]);
@@ -1925,6 +2088,29 @@ int grid_for(K kernel, int threads, int64_t work, int num_sms)
     return (int)(work < cap ? (work > 0 ? work : 1) : cap);
 }
 
+// The fast NES pass: 8-warp CTAs with the item table and the per-lane sums in
+// dynamic shared memory (two CTAs per SM).
+cudaError_t launch_nes_fast(const OpacityLaunch& L, int64_t p0, int64_t np, double* ws,
+                            cudaStream_t st, int sms)
+{
+    const int smem    = (int)sizeof(NesSmem);
+    cudaError_t e     = cudaFuncSetAttribute(grey_nes_fast_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess)
+        return e;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grey_nes_fast_kernel,
+                                                      kNesWarps * 32, smem) != cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    const int64_t work = (np + kNesWarps - 1) / kNesWarps;
+    int64_t cap        = (int64_t)((double)sms * per_sm * g_grid_scale);
+    cap                = cap < 1 ? 1 : cap;
+    const int grid     = (int)(work < cap ? (work > 0 ? work : 1) : cap);
+    grey_nes_fast_kernel<<<grid, kNesWarps * 32, smem, st>>>(L, p0, np, ws);
+    return cudaGetLastError();
+}
+
 template <bool MIXED>
 cudaError_t launch_brem(const OpacityLaunch& L, int64_t p0, int64_t np, double* ws,
                         cudaStream_t st, int sms, int add, int redo_only = 0)
@@ -1991,10 +2177,9 @@ __global__ void __launch_bounds__(128)
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
     {
-        const nes32::Geo G = nes32::make_geo(w[i], wp[i]);
         float I1, I2;
         double lref;
-        nes32::lepton_integrals(G, eta[i], I1, I2, lref);
+        nes32::lepton_integrals(w[i], wp[i], eta[i], I1, I2, lref);
         const double xy  = w[i] * wp[i];
         const double sgn = w[i] > wp[i] ? 1. : -1.;
         m1[i] = sgn * (double)I1 / (xy * xy);
@@ -2098,9 +2283,8 @@ cudaError_t launch_grey_chunks(const OpacityLaunch& L, cudaStream_t st0, cudaStr
             if (L.mixed)
             {
                 phase_mark(kPhNeps, 0, st);
-                grey_neps_kernel<kNesFast>
-                    <<<grid_for(grey_neps_kernel<kNesFast>, kWarps * 32, wb, sms), kWarps * 32, 0,
-                       st>>>(L, p0, np, wsk);
+                if ((err = launch_nes_fast(L, p0, np, wsk, st, sms)) != cudaSuccess)
+                    break;
                 phase_mark(kPhNeps, 1, st);
                 phase_mark(kPhNepsAccurate, 0, st);
                 grey_neps_kernel<kNesAccurate>
