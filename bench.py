@@ -819,10 +819,14 @@ def main():
         torch.distributed.barrier()
     bn.phase_times()
     bn.phase_timing(True)
+    bn.grey_mixed_stats(reset=True)
     launches0 = bn.kernel_launches()
     with ClockSampler(local) as clk:
         total_ms = timed_steps(step, args.steps, stream, torch)
     launches = bn.kernel_launches() - launches0
+    mstats = bn.grey_mixed_stats(reset=True)   # totals over the timed steps
+    fallbacks = ({k: v / max(1, mstats["evaluated"]) for k, v in mstats.items() if k != "evaluated"}
+                 if args.precision == "mixed" else None)
     bn.phase_timing(False)
     phases = bn.phase_times()
     if world > 1:
@@ -972,6 +976,7 @@ def main():
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "spectral": spectral,
             "clocks": clk.summary(), "gpu_launches": launches,
             "phases_ms": {k: {"ms": v[0], "launches": v[1]} for k, v in phases.items() if v[1]},
+            "fallback_fraction": fallbacks,
             "generator_s": gen_s,
         }
         print(json.dumps(line))

@@ -160,6 +160,7 @@ SIGNATURES = {
     "bnsn_spectral_mixed_stats": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64), ctypes.c_int]),
     "bnsn_distr_from_m1_point": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "bnsn_gp19_load_header": (ctypes.c_int, [ctypes.c_char_p]),
+    "bnsn_grey_mixed_stats": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64), ctypes.c_int]),
     "bnsn_nonfinite_outputs": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64), ctypes.c_int]),
     "bnsn_fdi": (c_int, [c_int, P, P, ctypes.c_int64, P]),
     "bnsn_pair_j_mixed": (c_int, [P, P, P, P, P, P, ctypes.c_int64, P]),

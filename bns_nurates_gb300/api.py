@@ -389,6 +389,15 @@ def spectral_mixed_stats(reset=False):
     return dict(zip(("evaluated", "fp64", "pb_fp64", "nes_fp64"), (int(v) for v in c)))
 
 
+def grey_mixed_stats(reset=False):
+    """Mixed grey path on the current device since the last reset:
+    {"evaluated", "nes_df", "nes_fp64", "pair_fp64", "brem_fp64"} point counts."""
+    c = (ctypes.c_int64 * 5)()
+    _check(C.load().bnsn_grey_mixed_stats(c, int(reset)))
+    return dict(zip(("evaluated", "nes_df", "nes_fp64", "pair_fp64", "brem_fp64"),
+                    (int(v) for v in c)))
+
+
 def nonfinite_outputs(reset=False):
     """Outputs with a NaN or Inf on the current device since the last reset:
     {"grey_points", "spectral_pairs"}."""

@@ -121,6 +121,7 @@ cudaError_t spectral_mixed_counts(unsigned long long* counts, bool reset);
 // Outputs holding a NaN or Inf since the last reset: grey points, spectral
 // (point, energy) pairs (synchronous reads of the current device's counters).
 cudaError_t grey_nonfinite_count(unsigned long long* count, bool reset);
+cudaError_t grey_mixed_counts(unsigned long long* counts, bool reset);
 cudaError_t spectral_nonfinite_count(unsigned long long* count, bool reset);
 struct DistrLaunch
 {

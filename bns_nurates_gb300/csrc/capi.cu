@@ -405,6 +405,22 @@ int bnsn_spectral_mixed_stats(int64_t* counts, int reset)
 }
 
 
+int bnsn_grey_mixed_stats(int64_t* counts, int reset)
+{
+    g_err.clear();
+    if (!counts)
+        return fail(BNSN_ERR_ARG, "NULL output");
+    unsigned long long c[5] = {0ull, 0ull, 0ull, 0ull, 0ull};
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess)
+        e = grey_mixed_counts(c, reset != 0);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "reading the grey mixed-path statistics");
+    for (int k = 0; k < 5; ++k)
+        counts[k] = (int64_t)c[k];
+    return BNSN_OK;
+}
+
 int bnsn_nonfinite_outputs(int64_t* counts, int reset)
 {
     g_err.clear();

@@ -87,6 +87,11 @@ struct PairMixed
     double predo;     // 1 if the point's pair sums must be recomputed in FP64
 };
 static_assert(sizeof(PairMixed) <= sizeof(((PointTab*)nullptr)->fm), "PairMixed overlay");
+// Mixed path: points evaluated, NES handed to the double-float pass, NES in
+// FP64, pair sums redone in FP64, brem sums redone in FP64 (read by
+// grey_mixed_counts).
+__device__ unsigned long long g_grey_mixed[5];
+
 __device__ __forceinline__ PairMixed* pair_mixed(PointTab* P)
 {
     return reinterpret_cast<PairMixed*>(&P->fm[0][0]);
@@ -486,19 +491,62 @@ struct Acc32
 // reconstructed occupation exceeds 1).  Terms are those of this lane (acc,
 // mag, unscaled; moments 8..15 scaled by scale_e); the result is
 // warp-reduced and 1 when every contribution has one sign.
-__device__ __forceinline__ double cancel_factor(const double* acc, const float* mag, double scale,
-                                                double scale_e, const double* other)
+// The same from the totals (already summed over the point's lanes).
+__device__ __forceinline__ double cancel_factor_tot(const double* acc, const double* mag,
+                                                    double scale, double scale_e,
+                                                    const double* other)
 {
     double amp = 1.;
 #pragma unroll
     for (int s = 0; s < 16; ++s)
     {
         const double sc  = s < 8 ? scale : scale_e;
-        const double m   = warp_sum((double)mag[s]) * sc;
-        const double tot = fabs(warp_sum(acc[s]) * sc + other[s]);
+        const double m   = mag[s] * sc;
+        const double tot = fabs(acc[s] * sc + other[s]);
         amp = fmax(amp, m > 0. ? m / tot : 1.);
     }
     return amp;
+}
+
+__device__ __forceinline__ double cancel_factor(const double* acc, const float* mag, double scale,
+                                                double scale_e, const double* other)
+{
+    double a[16], m[16];
+#pragma unroll
+    for (int s = 0; s < 16; ++s)
+    {
+        a[s] = warp_sum(acc[s]);
+        m[s] = warp_sum((double)mag[s]);
+    }
+    return cancel_factor_tot(a, m, scale, scale_e, other);
+}
+
+// v[0..16) summed over the CTA's NW warps in a fixed order; every thread
+// receives the totals.  red: NW x 32 doubles of shared memory, columns
+// col .. col + 15 used.
+template <int NW>
+__device__ __forceinline__ void block_sum(double* v, double (*red)[32], int col)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk)
+        v[kk] = warp_sum(v[kk]);
+    if (lane == 0)
+    {
+#pragma unroll
+        for (int kk = 0; kk < 16; ++kk)
+            red[wid][col + kk] = v[kk];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk)
+    {
+        double t = 0.;
+        for (int w = 0; w < NW; ++w)
+            t += red[w][col + kk];
+        v[kk] = t;
+    }
+    __syncthreads();
 }
 
 // The beta rates of a point in the units of the pair/brem sums (s2d, unit
@@ -692,16 +740,19 @@ __device__ __forceinline__ void pair_kernel_q(const PairTab32& X, int a, int b, 
 // s2d are written to the record (PairMixed).  !MIXED: the FP64 pair kernel
 // (kernel_pair.hpp), with redo_only the mixed path's second pass over the
 // points the final kernel marked (predo), whose pair part of s2d it replaces;
-// that pass computes its Fermi-integral tables itself.
-template <bool MIXED>
-__global__ void __launch_bounds__(kWarps * 32)
+// that pass computes its Fermi-integral tables itself.  WIDE (that pass):
+// a point per CTA, its cells over all threads (the marked points are few).
+template <bool MIXED, bool WIDE = false>
+__global__ void __launch_bounds__((WIDE ? 8 : kWarps) * 32)
     grey_pair_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
                      double* __restrict__ scratch, int redo_only)
 {
+    constexpr int NW = WIDE ? 8 : kWarps;
     __shared__ double s_A1[kMaxM], s_A2[kMaxM];
     __shared__ uint32_t s_cells[kMaxCells];
-    __shared__ CellTab s_ct[kWarps];
+    __shared__ CellTab s_ct[WIDE ? 1 : kWarps];
     __shared__ PairTab32 s_pt[MIXED ? kWarps : 1];
+    __shared__ double s_red[WIDE ? NW : 1][32];
     for (int k = threadIdx.x; k < kMaxM; k += blockDim.x)
     {
         s_A1[k]  = L.A1[k];
@@ -712,13 +763,17 @@ __global__ void __launch_bounds__(kWarps * 32)
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int wid  = threadIdx.x >> 5;
-    CellTab& C     = s_ct[wid];
+    CellTab& C     = s_ct[WIDE ? 0 : wid];
     PairTab32& X   = s_pt[MIXED ? wid : 0];
     const int M    = 2 * L.n2;
     const bool nbb = L.neglect_blocking != 0;
-    const int64_t nwarp = (int64_t)gridDim.x * kWarps;
+    // cells of a point: thread t0, t0 + stride, ...
+    const int t0        = WIDE ? (int)threadIdx.x : lane;
+    const int stride    = WIDE ? NW * 32 : 32;
+    const int64_t q0    = WIDE ? (int64_t)blockIdx.x : (int64_t)blockIdx.x * NW + wid;
+    const int64_t qstep = WIDE ? (int64_t)gridDim.x : (int64_t)gridDim.x * NW;
 
-    for (int64_t q = (int64_t)blockIdx.x * kWarps + wid; q < np; q += nwarp)
+    for (int64_t q = q0; q < np; q += qstep)
     {
         const int64_t p  = L.pidx ? L.pidx[p0 + q] : p0 + q;
         PointTab* P      = (PointTab*)(scratch + q * kTabWords);
@@ -726,8 +781,14 @@ __global__ void __launch_bounds__(kWarps * 32)
             continue;
         const double T   = L.eos[1][p];
         const double eta = L.eos[7][p] / T;
-        __syncwarp();
-        load_cell_tab(C, P, M, !MIXED && !redo_only, lane);
+        if (WIDE)
+            __syncthreads(); // the previous point's readers are done
+        else
+            __syncwarp();
+        if (!WIDE || wid == 0)
+            load_cell_tab(C, P, M, !MIXED && !redo_only, lane);
+        if (WIDE)
+            __syncthreads();
         if (MIXED)
         {
             __syncwarp();
@@ -744,7 +805,7 @@ __global__ void __launch_bounds__(kWarps * 32)
         if (!MIXED && redo_only)
         {
             // the F_1..F_5 tables the mixed prelude left out
-            for (int qq = lane; qq < 2 * M; qq += 32)
+            for (int qq = t0; qq < 2 * M; qq += stride)
             {
                 const int a = qq >> 1;
                 if (qq & 1)
@@ -753,8 +814,10 @@ __global__ void __launch_bounds__(kWarps * 32)
                     fdi_orders<1, 5>(eta - C.y[a], C.fm[a]);
             }
         }
-        __syncwarp();
-        __syncwarp();
+        if (WIDE)
+            __syncthreads();
+        else
+            __syncwarp();
         double acc[16], magem[MIXED ? 8 : 1];
 #pragma unroll
         for (int kk = 0; kk < 16; ++kk)
@@ -765,7 +828,7 @@ __global__ void __launch_bounds__(kWarps * 32)
         const dfm::df ETA = dfm::from_double(eta);
         const double T2 = T * T;
         const double scq = 0.5 * k::PairPhi * T2 * (T2 * T2) / 15.;
-        for (int c = lane; c < L.ncell; c += 32)
+        for (int c = t0; c < L.ncell; c += stride)
         {
             const uint32_t ab = s_cells[c];
             const int a = ab & 0xffffu, b = ab >> 16;
@@ -817,9 +880,14 @@ __global__ void __launch_bounds__(kWarps * 32)
             }
         }
         double magd[16];
+        if (WIDE)
+            block_sum<NW>(acc, s_red, 0);
+        else
+        {
 #pragma unroll
-        for (int kk = 0; kk < 16; ++kk)
-            acc[kk] = warp_sum(acc[kk]);
+            for (int kk = 0; kk < 16; ++kk)
+                acc[kk] = warp_sum(acc[kk]);
+        }
         if (MIXED)
         {
             // emission moments: sum of |term|; absorption terms are non-negative
@@ -832,7 +900,7 @@ __global__ void __launch_bounds__(kWarps * 32)
                 magd[12 + s] = fabs(acc[12 + s]);
             }
         }
-        if (lane == 0)
+        if (WIDE ? threadIdx.x == 0 : lane == 0)
         {
             PairMixed* X = pair_mixed(P);
 #pragma unroll
@@ -864,17 +932,22 @@ struct Gp19Warp
 };
 
 // IMPL: 0 HR98, 1 BRT06, 2 GP19.  ADD: accumulate onto the pair sums.
-template <bool MIXED, int IMPL>
-__global__ void __launch_bounds__(kWarps * 32)
+// WIDE (the mixed path's FP64 pass over the few marked points): a point per
+// CTA, its cells over all threads.
+template <bool MIXED, int IMPL, bool WIDE = false>
+__global__ void __launch_bounds__((WIDE ? 8 : kWarps) * 32)
     grey_brem_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
                      double* __restrict__ scratch, int add, int redo_only)
 {
+    constexpr int NW = WIDE ? 8 : kWarps;
+    constexpr int NT = WIDE ? 1 : kWarps; // point tables in flight per CTA
     __shared__ double s_A1[kMaxM], s_A2[kMaxM];
     __shared__ dfm::df s_A1d[MIXED ? kMaxM : 1], s_A2d[MIXED ? kMaxM : 1];
     __shared__ uint32_t s_cells[kMaxCells];
-    __shared__ CellTab s_ct[kWarps];
+    __shared__ CellTab s_ct[NT];
     __shared__ CellTab32 s_c32[MIXED ? kWarps : 1];
-    __shared__ Gp19Warp s_gw[IMPL == 2 ? kWarps : 1];
+    __shared__ Gp19Warp s_gw[IMPL == 2 ? NT : 1];
+    __shared__ double s_red[WIDE ? NW : 1][32];
     __shared__ double s_lw[IMPL == 2 ? kGp19MaxW : 1];
     __shared__ float s_lwf[IMPL == 2 ? kGp19MaxW : 1];
     constexpr int kWF = (IMPL == 2 && MIXED) ? kGp19MaxW : 1;
@@ -910,42 +983,62 @@ __global__ void __launch_bounds__(kWarps * 32)
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int wid  = threadIdx.x >> 5;
-    CellTab& C     = s_ct[wid];
+    CellTab& C     = s_ct[WIDE ? 0 : wid];
     const int M    = 2 * L.n2;
     const bool nbb = L.neglect_blocking != 0;
-    const int64_t nwarp = (int64_t)gridDim.x * kWarps;
+    // cells of a point: thread t0, t0 + stride, ...
+    const int t0        = WIDE ? (int)threadIdx.x : lane;
+    const int stride    = WIDE ? NW * 32 : 32;
+    const int64_t q0    = WIDE ? (int64_t)blockIdx.x : (int64_t)blockIdx.x * NW + wid;
+    const int64_t qstep = WIDE ? (int64_t)gridDim.x : (int64_t)gridDim.x * NW;
     const double wmin = IMPL == 2 ? G19.w[0] : 0., wmax = IMPL == 2 ? G19.w[G19.d3 - 1] : 0.;
 
-    for (int64_t q = (int64_t)blockIdx.x * kWarps + wid; q < np; q += nwarp)
+    for (int64_t q = q0; q < np; q += qstep)
     {
         const int64_t p = L.pidx ? L.pidx[p0 + q] : p0 + q;
         PointTab* P     = (PointTab*)(scratch + q * kTabWords);
         if (redo_only && P->bredo != 1.)
-            continue; // warp-uniform: one point per warp
+            continue; // uniform: one point per warp (per CTA when WIDE)
         const double T  = L.eos[1][p];
-        __syncwarp();
-        load_cell_tab(C, P, M, false, lane);
-        if (IMPL == 0)
-            warp_copy((double*)&C.hr, (const double*)&P->hr, sizeof(Hr98Point) / sizeof(double),
-                      lane);
-        __syncwarp();
+        if (WIDE)
+            __syncthreads(); // the previous point's readers are done
+        else
+            __syncwarp();
+        if (!WIDE || wid == 0)
+        {
+            load_cell_tab(C, P, M, false, lane);
+            if (IMPL == 0)
+                warp_copy((double*)&C.hr, (const double*)&P->hr,
+                          sizeof(Hr98Point) / sizeof(double), lane);
+        }
+        if (WIDE)
+            __syncthreads();
+        else
+            __syncwarp();
         if (IMPL == 0 && MIXED && lane == 0)
             fp32::hr98_mixed_from(C.hr, &C.hm);
         const double nbp = L.eos[0][p], yep = L.eos[2][p];
-        Gp19Warp& GW     = s_gw[IMPL == 2 ? wid : 0];
+        Gp19Warp& GW     = s_gw[IMPL == 2 && !WIDE ? wid : 0];
         if (IMPL == 2 && prof)
         {
-            if (lane == 0)
+            if (WIDE ? threadIdx.x == 0 : lane == 0)
                 gp19_point(G19, nbp, yep, T, &GW.pt);
-            __syncwarp();
+            if (WIDE)
+                __syncthreads();
+            else
+                __syncwarp();
             const int np19 = (GW.pt.regime >= 2) ? 2 : 1;
-            for (int e = lane; e < np19 * G19.d3; e += 32)
+            for (int e = t0; e < np19 * G19.d3; e += stride)
             {
                 const int pr = e / G19.d3, l = e - pr * G19.d3;
                 const double v = gp19_profile_at(G19, GW.pt.nbp, GW.pt.yep, GW.pt.pT[pr], l);
                 GW.p[pr][l]  = v;
                 GW.pf[pr][l] = (float)v;
             }
+            if (WIDE)
+                __syncthreads();
+            else
+                __syncwarp();
         }
         // Mixed cells in FP32 except BRT06, the GP19 high-T extrapolation and
         // points whose pair sums are negative somewhere: there the outputs
@@ -1070,7 +1163,7 @@ __global__ void __launch_bounds__(kWarps * 32)
         }
         if (!fp32_cells || redo)
         {
-            for (int c = lane; c < L.ncell; c += 32)
+            for (int c = t0; c < L.ncell; c += stride)
             {
                 const uint32_t ab = s_cells[c];
                 const int a = ab & 0xffffu, b = ab >> 16;
@@ -1112,10 +1205,15 @@ __global__ void __launch_bounds__(kWarps * 32)
                 }
             }
         }
+        if (WIDE)
+            block_sum<NW>(acc, s_red, 0);
+        else
+        {
 #pragma unroll
-        for (int kk = 0; kk < 16; ++kk)
-            acc[kk] = warp_sum(acc[kk]);
-        if (lane == 0)
+            for (int kk = 0; kk < 16; ++kk)
+                acc[kk] = warp_sum(acc[kk]);
+        }
+        if (WIDE ? threadIdx.x == 0 : lane == 0)
         {
             // a redo replaces the FP32 brem part of s2d by the FP64 one
 #pragma unroll
@@ -1163,10 +1261,10 @@ __device__ __forceinline__ void neps_items_fp64(const NepsPoint& NP, const Distr
                                                 int n2, double tn, bool stim, bool nbb,
                                                 const double* s_x2, const double* s_w2,
                                                 const double* s_wx, const double* s_wx3,
-                                                int lane, double* acc)
+                                                int t0, int stride, double* acc)
 {
     const int nn2 = n2 * n2;
-    for (int it = lane; it < 2 * nn2; it += 32)
+    for (int it = t0; it < 2 * nn2; it += stride)
     {
         const int r   = it >= nn2;
         const int rem = it - r * nn2;
@@ -1346,16 +1444,30 @@ enum NesMode
     kNesFp64Flag
 };
 
+// Warps per CTA of the NES kernels: the plain path runs a point per warp; the
+// mixed path's passes over the few points flagged by the fast pass run a
+// point per CTA, its items over all the CTA's threads (one warp alone would
+// leave the pass as long as a point's whole item loop).
 template <int MODE>
-__global__ void __launch_bounds__(kWarps * 32, MODE == kNesAccurate ? 4 : 1)
+__host__ __device__ constexpr int nes_warps()
+{
+    return MODE == kNesFp64All ? kWarps : 8;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(nes_warps<MODE>() * 32, MODE == kNesAccurate ? 2 : 1)
     grey_neps_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
                      double* __restrict__ scratch)
 {
-    constexpr bool MIX = MODE == kNesAccurate;
+    constexpr bool MIX  = MODE == kNesAccurate;
+    constexpr bool WIDE = MODE != kNesFp64All;  // a point per CTA
+    constexpr int NW    = nes_warps<MODE>();
+    constexpr int NT    = WIDE ? 1 : NW;        // point tables in flight per CTA
     __shared__ double s_x2[kMaxQ], s_w2[kMaxQ], s_wx[kMaxQ], s_wx3[kMaxQ];
-    __shared__ NepsTab s_nt[kWarps];
-    __shared__ NepsMixed s_nm[MIX ? kWarps : 1];
+    __shared__ NepsTab s_nt[NT];
+    __shared__ NepsMixed s_nm[MIX ? NT : 1];
     __shared__ dfm::FdiTab s_ftab;
+    __shared__ double s_red[WIDE ? NW : 1][32];
     for (int k = threadIdx.x; k < kMaxQ; k += blockDim.x)
     {
         s_x2[k]  = L.x2[k];
@@ -1369,12 +1481,16 @@ __global__ void __launch_bounds__(kWarps * 32, MODE == kNesAccurate ? 4 : 1)
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int wid  = threadIdx.x >> 5;
-    NepsTab& N     = s_nt[wid];
+    NepsTab& N     = s_nt[WIDE ? 0 : wid];
     const int n2   = L.n2;
     const bool nbb = L.neglect_blocking != 0;
-    const int64_t nwarp = (int64_t)gridDim.x * kWarps;
+    // items of a point: thread t0, t0 + stride, ...
+    const int t0     = WIDE ? (int)threadIdx.x : lane;
+    const int stride = WIDE ? NW * 32 : 32;
+    const int64_t q0    = WIDE ? (int64_t)blockIdx.x : (int64_t)blockIdx.x * NW + wid;
+    const int64_t qstep = WIDE ? (int64_t)gridDim.x : (int64_t)gridDim.x * NW;
 
-    for (int64_t q = (int64_t)blockIdx.x * kWarps + wid; q < np; q += nwarp)
+    for (int64_t q = q0; q < np; q += qstep)
     {
         const int64_t p = L.pidx ? L.pidx[p0 + q] : p0 + q;
         PointTab* P     = (PointTab*)(scratch + q * kTabWords);
@@ -1383,11 +1499,20 @@ __global__ void __launch_bounds__(kWarps * 32, MODE == kNesAccurate ? 4 : 1)
         if (MODE == kNesFp64Flag && P->neps_fp64 != 2.)
             continue;
         const double T = L.eos[1][p], mu_e = L.eos[7][p];
-        __syncwarp();
-        warp_copy((double*)&N.d, (const double*)&P->d, 28 + 12 + 2, lane);
-        if (lane == 0)
-            N.same_cf = P->same_cf;
-        __syncwarp();
+        if (WIDE)
+            __syncthreads(); // the previous point's readers are done
+        else
+            __syncwarp();
+        if (!WIDE || wid == 0)
+        {
+            warp_copy((double*)&N.d, (const double*)&P->d, 28 + 12 + 2, lane);
+            if (lane == 0)
+                N.same_cf = P->same_cf;
+        }
+        if (WIDE)
+            __syncthreads();
+        else
+            __syncwarp();
         const bool same_cf = N.same_cf != 0.;
         NepsPoint NP;
         NP.T    = T;
@@ -1406,19 +1531,19 @@ __global__ void __launch_bounds__(kWarps * 32, MODE == kNesAccurate ? 4 : 1)
         if (!MIX)
         {
             neps_items_fp64(NP, N.d, same_cf, n2, tn, L.stim != 0, nbb, s_x2, s_w2, s_wx, s_wx3,
-                            lane, acc);
+                            t0, stride, acc);
         }
         else
         {
             int flag = 0;
             {
-                NepsMixed& Q = s_nm[MIX ? wid : 0];
-                if (lane < 2)
+                NepsMixed& Q = s_nm[WIDE ? 0 : wid];
+                if ((!WIDE || wid == 0) && lane < 2)
                 {
                     Q.eta[lane] = dfm::from_double(lane ? NP.eta1 : NP.eta0);
                     dfm::fdi_raw15(Q.eta[lane], Q.reta[lane], 1, &s_ftab);
                 }
-                else if (lane >= 8 && lane < 12)
+                else if ((!WIDE || wid == 0) && lane >= 8 && lane < 12)
                 {
                     const int s    = lane - 8;
                     const Distr& d = N.d;
@@ -1428,7 +1553,10 @@ __global__ void __launch_bounds__(kWarps * 32, MODE == kNesAccurate ? 4 : 1)
                     Q.invTf[s] = 1. / d.temp_f[s];
                     Q.cf[s]    = d.c_f[s];
                 }
-                __syncwarp();
+                if (WIDE)
+                    __syncthreads();
+                else
+                    __syncwarp();
                 const double invT = 1. / T;
                 const double lhtn = log(0.5 * tn);
                 dfm::df dacc[16];
@@ -1440,7 +1568,7 @@ __global__ void __launch_bounds__(kWarps * 32, MODE == kNesAccurate ? 4 : 1)
                 for (int kk = 0; kk < 16; ++kk)
                     mag[kk] = 0.f;
                 const int nn2 = n2 * n2;
-                for (int it = lane; it < 2 * nn2; it += 32)
+                for (int it = t0; it < 2 * nn2; it += stride)
                 {
                     const int r   = it >= nn2;
                     const int rem = it - r * nn2;
@@ -1522,7 +1650,26 @@ __global__ void __launch_bounds__(kWarps * 32, MODE == kNesAccurate ? 4 : 1)
                     other[kk] += (L.use_pair || L.use_brem)
                                      ? 0.125 * P->s2d[kk] * (kk >= 8 ? t2d : 1.)
                                      : 0.;
-                const double amp = cancel_factor(acc, mag, NP.pre * T4, NP.pre * T4 * T, other);
+                double macc[16];
+#pragma unroll
+                for (int kk = 0; kk < 16; ++kk)
+                    macc[kk] = (double)mag[kk];
+                if (WIDE)
+                {
+                    block_sum<NW>(acc, s_red, 0);
+                    block_sum<NW>(macc, s_red, 16);
+                }
+                else
+                {
+#pragma unroll
+                    for (int kk = 0; kk < 16; ++kk)
+                    {
+                        acc[kk]  = warp_sum(acc[kk]);
+                        macc[kk] = warp_sum(macc[kk]);
+                    }
+                }
+                const double amp =
+                    cancel_factor_tot(acc, macc, NP.pre * T4, NP.pre * T4 * T, other);
                 if (amp > kMaxCancelDf)
                     flag = 2;
 #pragma unroll
@@ -1531,16 +1678,26 @@ __global__ void __launch_bounds__(kWarps * 32, MODE == kNesAccurate ? 4 : 1)
             }
             if (flag != 0)
             {
-                if (lane == 0)
+                if (WIDE ? threadIdx.x == 0 : lane == 0)
+                {
                     P->neps_fp64 = (double)flag;
-            }
-            if (flag != 0)
+                    atomicAdd(&g_grey_mixed[2], 1ull);
+                }
                 continue; // a later launch writes this point's sums
+            }
         }
+        if (!MIX) // (the mixed pass has summed over the point's threads already)
+        {
+            if (WIDE)
+                block_sum<NW>(acc, s_red, 0);
+            else
+            {
 #pragma unroll
-        for (int kk = 0; kk < 16; ++kk)
-            acc[kk] = warp_sum(acc[kk]);
-        if (lane == 0)
+                for (int kk = 0; kk < 16; ++kk)
+                    acc[kk] = warp_sum(acc[kk]);
+            }
+        }
+        if (WIDE ? threadIdx.x == 0 : lane == 0)
         {
 #pragma unroll
             for (int kk = 0; kk < 16; ++kk)
@@ -1936,7 +2093,11 @@ __global__ void __launch_bounds__(kNesWarps * 32, 2)
                 acc[kk] *= NP.pre * T4 * (kk >= 8 ? T : 1.);
         }
         if (lane == 0)
+        {
             P->neps_fp64 = (double)flag;
+            if (flag != 0)
+                atomicAdd(&g_grey_mixed[flag], 1ull);
+        }
         if (flag != 0)
             continue; // a later launch writes this point's sums
 #pragma unroll
@@ -2066,6 +2227,14 @@ __global__ void __launch_bounds__(128)
             P->bredo = bredo ? 1. : 0.;
         if (check_pair)
             pair_mixed(P)->predo = predo ? 1. : 0.;
+        if (!redo_only && L.mixed)
+        {
+            atomicAdd(&g_grey_mixed[0], 1ull);
+            if (predo)
+                atomicAdd(&g_grey_mixed[3], 1ull);
+            if (bredo)
+                atomicAdd(&g_grey_mixed[4], 1ull);
+        }
         if (nonfinite && !redo_only)
             atomicAdd(&g_grey_nonfinite, 1ull);
     }
@@ -2111,24 +2280,46 @@ cudaError_t launch_nes_fast(const OpacityLaunch& L, int64_t p0, int64_t np, doub
     return cudaGetLastError();
 }
 
+template <bool MIXED, int IMPL, bool WIDE>
+void launch_brem_impl(const OpacityLaunch& L, int64_t p0, int64_t np, double* ws,
+                      cudaStream_t st, int sms, int add, int redo_only)
+{
+    constexpr int threads = (WIDE ? 8 : kWarps) * 32;
+    const int64_t work    = WIDE ? np : (np + kWarps - 1) / kWarps;
+    grey_brem_kernel<MIXED, IMPL, WIDE>
+        <<<grid_for(grey_brem_kernel<MIXED, IMPL, WIDE>, threads, work, sms), threads, 0, st>>>(
+            L, p0, np, ws, add, redo_only);
+}
+
+// redo_only (the FP64 pass over the points the final kernel marked) runs a
+// point per CTA.
 template <bool MIXED>
 cudaError_t launch_brem(const OpacityLaunch& L, int64_t p0, int64_t np, double* ws,
                         cudaStream_t st, int sms, int add, int redo_only = 0)
 {
-    const int64_t wb = (np + kWarps - 1) / kWarps;
     phase_mark(kPhBrem, 0, st);
-    if (L.brem_impl == 0)
-        grey_brem_kernel<MIXED, 0>
-            <<<grid_for(grey_brem_kernel<MIXED, 0>, kWarps * 32, wb, sms), kWarps * 32, 0, st>>>(
-                L, p0, np, ws, add, redo_only);
+    bool done = false;
+    if constexpr (!MIXED)
+    {
+        if (redo_only)
+        {
+            if (L.brem_impl == 0)
+                launch_brem_impl<false, 0, true>(L, p0, np, ws, st, sms, add, redo_only);
+            else if (L.brem_impl == 1)
+                launch_brem_impl<false, 1, true>(L, p0, np, ws, st, sms, add, redo_only);
+            else
+                launch_brem_impl<false, 2, true>(L, p0, np, ws, st, sms, add, redo_only);
+            done = true;
+        }
+    }
+    if (done)
+        ;
+    else if (L.brem_impl == 0)
+        launch_brem_impl<MIXED, 0, false>(L, p0, np, ws, st, sms, add, redo_only);
     else if (L.brem_impl == 1)
-        grey_brem_kernel<MIXED, 1>
-            <<<grid_for(grey_brem_kernel<MIXED, 1>, kWarps * 32, wb, sms), kWarps * 32, 0, st>>>(
-                L, p0, np, ws, add, redo_only);
+        launch_brem_impl<MIXED, 1, false>(L, p0, np, ws, st, sms, add, redo_only);
     else
-        grey_brem_kernel<MIXED, 2>
-            <<<grid_for(grey_brem_kernel<MIXED, 2>, kWarps * 32, wb, sms), kWarps * 32, 0, st>>>(
-                L, p0, np, ws, add, redo_only);
+        launch_brem_impl<MIXED, 2, false>(L, p0, np, ws, st, sms, add, redo_only);
     phase_mark(kPhBrem, 1, st);
     return cudaGetLastError();
 }
@@ -2216,6 +2407,17 @@ cudaError_t launch_pair_j(const double* y, const double* z, const double* eta, d
     return cudaGetLastError();
 }
 
+cudaError_t grey_mixed_counts(unsigned long long* counts, bool reset)
+{
+    cudaError_t e = cudaMemcpyFromSymbol(counts, g_grey_mixed, 5 * sizeof(*counts));
+    if (e == cudaSuccess && reset)
+    {
+        const unsigned long long zero[5] = {0ull, 0ull, 0ull, 0ull, 0ull};
+        e = cudaMemcpyToSymbol(g_grey_mixed, zero, sizeof(zero));
+    }
+    return e;
+}
+
 cudaError_t grey_nonfinite_count(unsigned long long* count, bool reset)
 {
     cudaError_t e = cudaMemcpyFromSymbol(count, g_grey_nonfinite, sizeof(*count));
@@ -2288,12 +2490,16 @@ cudaError_t launch_grey_chunks(const OpacityLaunch& L, cudaStream_t st0, cudaStr
                 phase_mark(kPhNeps, 1, st);
                 phase_mark(kPhNepsAccurate, 0, st);
                 grey_neps_kernel<kNesAccurate>
-                    <<<grid_for(grey_neps_kernel<kNesAccurate>, kWarps * 32, wb, sms), kWarps * 32,
+                    <<<grid_for(grey_neps_kernel<kNesAccurate>, nes_warps<kNesAccurate>() * 32, np,
+                                sms),
+                       nes_warps<kNesAccurate>() * 32,
                        0, st>>>(L, p0, np, wsk);
                 phase_mark(kPhNepsAccurate, 1, st);
                 phase_mark(kPhNepsFp64, 0, st);
                 grey_neps_kernel<kNesFp64Flag>
-                    <<<grid_for(grey_neps_kernel<kNesFp64Flag>, kWarps * 32, wb, sms), kWarps * 32,
+                    <<<grid_for(grey_neps_kernel<kNesFp64Flag>, nes_warps<kNesFp64Flag>() * 32, np,
+                                sms),
+                       nes_warps<kNesFp64Flag>() * 32,
                        0, st>>>(L, p0, np, wsk);
                 phase_mark(kPhNepsFp64, 1, st);
             }
@@ -2317,8 +2523,9 @@ cudaError_t launch_grey_chunks(const OpacityLaunch& L, cudaStream_t st0, cudaStr
             if (L.use_pair)
             {
                 phase_mark(kPhPair, 0, st);
-                grey_pair_kernel<false><<<grid_for(grey_pair_kernel<false>, kWarps * 32, wb, sms),
-                                          kWarps * 32, 0, st>>>(L, p0, np, wsk, 1);
+                grey_pair_kernel<false, true>
+                    <<<grid_for(grey_pair_kernel<false, true>, 8 * 32, np, sms), 8 * 32, 0, st>>>(
+                        L, p0, np, wsk, 1);
                 phase_mark(kPhPair, 1, st);
             }
             if (L.use_brem &&

@@ -524,6 +524,16 @@ int64_t bnsn_kernel_launches(void);
  * synchronises the device.  A diagnostic with no counterpart in the
  * reference. */
 int bnsn_spectral_mixed_stats(int64_t* counts, int reset);
+/* Mixed-precision grey path on the current device since the last reset:
+ * counts[0] points evaluated, counts[1] points whose NES/NPS sums went to the
+ * double-float pass (their FP32 terms cancel), counts[2] points whose NES sums
+ * were computed in FP64 (outside the FP32 range envelope, or cancelling
+ * beyond the double-float pass), counts[3] points whose pair sums and
+ * counts[4] points whose brem sums were recomputed in FP64 (cancellation
+ * against the other reactions).  reset != 0 zeroes the counters after
+ * reading; synchronises the device.  A diagnostic with no counterpart in the
+ * reference. */
+int bnsn_grey_mixed_stats(int64_t* counts, int reset);
 /* Outputs holding a NaN or Inf on the current device since the last reset:
  * counts[0] grey points (any of the 20 outputs), counts[1] spectral (point,
  * energy) pairs (any of the 16 outputs).  The kernels never trap: non-finite

@@ -57,3 +57,22 @@ def test_spectral_mixed_stats_count_every_pair(cuda):
     assert st["evaluated"] == 300 * 24
     assert st["fp64"] < st["evaluated"] // 2
     assert st["fp64"] <= st["pb_fp64"] + st["nes_fp64"]
+
+
+def test_grey_mixed_stats_count_every_point(cuda):
+    """The mixed grey path counts its points and the ones it hands to the
+    double-float and FP64 passes; the plain path counts nothing."""
+    eos, m1 = bn.synthetic_points(23, 500)
+    e, m = cuda.from_numpy(eos).cuda(), cuda.from_numpy(m1).cuda()
+    flags = bn.opacity_flags(use_abs_em=1, use_pair=1, use_brem=1, use_inelastic_scatt=1,
+                             use_iso=1)
+    bn.grey_mixed_stats(reset=True)
+    bn.m1_opacities(e, m, flags, _params(0), bn.gauss_legendre(10), precision="fp64")
+    assert bn.grey_mixed_stats()["evaluated"] == 0
+    bn.m1_opacities(e, m, flags, _params(0), bn.gauss_legendre(10), precision="mixed")
+    st = bn.grey_mixed_stats(reset=True)
+    assert st["evaluated"] == 500
+    for k in ("nes_df", "nes_fp64", "pair_fp64", "brem_fp64"):
+        assert 0 <= st[k] < 250, (k, st)
+    assert bn.grey_mixed_stats() == {"evaluated": 0, "nes_df": 0, "nes_fp64": 0,
+                                     "pair_fp64": 0, "brem_fp64": 0}
