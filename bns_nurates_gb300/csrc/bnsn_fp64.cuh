@@ -1035,26 +1035,50 @@ BNSN_DI void gp19_point(const Gp19Table& G, double nb_nm, double ye_in, double T
     }
 }
 
-// Profile entry at w column l for the (nb', Ye', T') of a point; NaN where
-// the reference's interpolation brackets fail.
-BNSN_DI double gp19_profile_at(const Gp19Table& G, double nbp, double yep, double Tp, int l)
+// The (nb', Ye', T') corner of the table and the 8 trilinear weights of a
+// profile, the same for every w column: the brackets are found once per
+// profile instead of once per entry.  ok = 0 where the reference's
+// interpolation brackets fail.
+struct Gp19Corners
+{
+    int64_t base; // offset of corner (i, j, k) at column 0
+    double w[8];  // weights of (di, dj, dk) = (0,0,0), (0,0,1), (0,1,0), ..., (1,1,1)
+    int ok;
+};
+
+BNSN_DI void gp19_profile_corners(const Gp19Table& G, double nbp, double yep, double Tp,
+                                  Gp19Corners* C)
 {
     double tx, ty, tz;
     const int i  = gp19_bracket(log(nbp), G.lognb, G.d0, &tx);
     const int j  = gp19_bracket(yep, G.ye, G.d1, &ty);
     const int kk = gp19_bracket(Tp, G.t, G.d2, &tz);
-    if (i < 0 || j < 0 || kk < 0)
-        return __longlong_as_double(0x7ff8000000000000LL);
-    const double* g = G.data;
-    const int D1 = G.d1, D2 = G.d2, D3 = G.d3;
-    auto at = [&](int a, int b, int c) {
-        return __ldg(&g[(((int64_t)(a) * D1 + b) * D2 + c) * D3 + l]);
-    };
+    C->ok = i >= 0 && j >= 0 && kk >= 0;
+    if (!C->ok)
+        return;
+    C->base = (((int64_t)i * G.d1 + j) * G.d2 + kk) * G.d3;
     const double a0 = 1. - tx, a1 = tx, b0 = 1. - ty, b1 = ty, c0 = 1. - tz, c1 = tz;
-    return at(i, j, kk) * a0 * b0 * c0 + at(i, j, kk + 1) * a0 * b0 * c1 +
-           at(i, j + 1, kk) * a0 * b1 * c0 + at(i, j + 1, kk + 1) * a0 * b1 * c1 +
-           at(i + 1, j, kk) * a1 * b0 * c0 + at(i + 1, j, kk + 1) * a1 * b0 * c1 +
-           at(i + 1, j + 1, kk) * a1 * b1 * c0 + at(i + 1, j + 1, kk + 1) * a1 * b1 * c1;
+    C->w[0] = a0 * b0 * c0;
+    C->w[1] = a0 * b0 * c1;
+    C->w[2] = a0 * b1 * c0;
+    C->w[3] = a0 * b1 * c1;
+    C->w[4] = a1 * b0 * c0;
+    C->w[5] = a1 * b0 * c1;
+    C->w[6] = a1 * b1 * c0;
+    C->w[7] = a1 * b1 * c1;
+}
+
+// Profile entry at w column l: the trilinear interpolation in (nb, Ye, T) of
+// the reference (kernel_brem_GP19.hpp); NaN where the brackets fail.
+BNSN_DI double gp19_profile_eval(const Gp19Table& G, const Gp19Corners& C, int l)
+{
+    if (!C.ok)
+        return __longlong_as_double(0x7ff8000000000000LL);
+    const int64_t S2 = G.d3, S1 = (int64_t)G.d2 * G.d3, S0 = (int64_t)G.d1 * S1;
+    const double* g = G.data + C.base + l;
+    return __ldg(g) * C.w[0] + __ldg(g + S2) * C.w[1] + __ldg(g + S1) * C.w[2] +
+           __ldg(g + S1 + S2) * C.w[3] + __ldg(g + S0) * C.w[4] + __ldg(g + S0 + S2) * C.w[5] +
+           __ldg(g + S0 + S1) * C.w[6] + __ldg(g + S0 + S1 + S2) * C.w[7];
 }
 
 // The high-temperature extrapolation (kernel_brem_GP19.hpp:285-355) from the

@@ -927,6 +927,7 @@ __global__ void __launch_bounds__((WIDE ? 8 : kWarps) * 32)
 struct Gp19Warp
 {
     Gp19Point pt;
+    Gp19Corners cor[2];
     double p[2][kGp19MaxW];
     float pf[2][kGp19MaxW];
 };
@@ -1028,10 +1029,16 @@ __global__ void __launch_bounds__((WIDE ? 8 : kWarps) * 32)
             else
                 __syncwarp();
             const int np19 = (GW.pt.regime >= 2) ? 2 : 1;
+            if (t0 < np19)
+                gp19_profile_corners(G19, GW.pt.nbp, GW.pt.yep, GW.pt.pT[t0], &GW.cor[t0]);
+            if (WIDE)
+                __syncthreads();
+            else
+                __syncwarp();
             for (int e = t0; e < np19 * G19.d3; e += stride)
             {
                 const int pr = e / G19.d3, l = e - pr * G19.d3;
-                const double v = gp19_profile_at(G19, GW.pt.nbp, GW.pt.yep, GW.pt.pT[pr], l);
+                const double v = gp19_profile_eval(G19, GW.cor[pr], l);
                 GW.p[pr][l]  = v;
                 GW.pf[pr][l] = (float)v;
             }

@@ -207,6 +207,7 @@ struct PbWarp
     double fmz[kMaxM][5], fpz[kMaxM][5];
     double fmy[kEChunk][5], fpy[kEChunk][5];
     Gp19Point gp;
+    Gp19Corners gc[2];
     double gpp[2][kGp19MaxW];
 };
 
@@ -329,10 +330,13 @@ __global__ void __launch_bounds__(kWarps * 32)
         if (prof)
         {
             const int np19 = (W.gp.regime >= 2) ? 2 : 1;
+            if (lane < np19)
+                gp19_profile_corners(G19, W.gp.nbp, W.gp.yep, W.gp.pT[lane], &W.gc[lane]);
+            __syncwarp();
             for (int e = lane; e < np19 * G19.d3; e += 32)
             {
                 const int pr = e / G19.d3, l = e - pr * G19.d3;
-                const double v = gp19_profile_at(G19, W.gp.nbp, W.gp.yep, W.gp.pT[pr], l);
+                const double v = gp19_profile_eval(G19, W.gc[pr], l);
                 W.gpp[pr][l] = v;
                 if (MIX)
                     X.gp32[pr][l] = (float)v;
