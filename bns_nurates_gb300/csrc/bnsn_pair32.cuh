@@ -132,7 +132,9 @@ __device__ __forceinline__ void edge_panel(int k, const Cell& c, dfm::df pu, dfm
         const bool n1 = d1 < 0.f, p2 = d2 > 0.f;
         const float arg = n1 ? k10 + ht : (p2 ? k01 - ht : c.k00);
         const float corr = (1.f + __expf(-fabsf(d1))) * (1.f + __expf(-fabsf(d2)));
-        const float gh   = __expf(arg) / corr;
+        float rc;  // 1 / corr, corr in [1, 4]: approximate reciprocal (1 ulp)
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rc) : "f"(corr));
+        const float gh = __expf(arg) * rc;
         float h0, h1;
         hpair(k, c, CM.hi + ht, rq - ht, h0, h1);
         const float w = kG8w[i >> 1] * gh;
