@@ -15,7 +15,7 @@ from .api import (BlocksPlan, BnsnError, ComputeM1Opacities, ComputeM1OpacitiesN
                   fp32_peak_tflops, fp64_peak_tflops, gauss_legendre, gp19_table_from_header,
                   grey_mixed_stats,
                   kernel_launches, load_gp19_header, m1_opacities,
-                  m1_opacities_host, nonfinite_outputs, nu_equilibrium, opacity_flags, opacity_params, params_tuple,
+                  m1_opacities_grid_boxes, m1_opacities_host, nonfinite_outputs, nu_equilibrium, opacity_flags, opacity_params, params_tuple,
                   nes_m_mixed, pair_j_mixed, phase_times, phase_timing, quad_arrays, set_gp19_table, spectral_mixed_stats,
                   spectral_opacities, synthetic_points)
 

@@ -123,6 +123,11 @@ class DistrSoA(ctypes.Structure):
     _fields_ = [(n, P * 4) for n in ("w_t", "temp_t", "eta_t", "w_f", "temp_f", "c_f", "beta_f")]
 
 
+class GridBox(ctypes.Structure):
+    _fields_ = [("shape", ctypes.c_int64 * 3), ("lo", ctypes.c_int64 * 3),
+                ("hi", ctypes.c_int64 * 3), ("eos", P * 11), ("m1", P * 12), ("out", P * 20)]
+
+
 class M1OpacitiesSoA(ctypes.Structure):
     _fields_ = [(n, P * 4) for n in ("eta_0", "kappa_0_a", "eta", "kappa_a", "kappa_s")]
 
@@ -134,6 +139,7 @@ class SpectralSoA(ctypes.Structure):
 # every entry point of the header, with its ctypes signature
 SIGNATURES = {
     "bnsn_m1_opacities": (c_int, [P, P, P, P, P, P, P, c_int, c_int, P, ctypes.c_int64, P]),
+    "bnsn_m1_opacities_grid_boxes": (c_int, [P, P, P, P, P, c_int, P, P, c_int, c_int, P]),
     "bnsn_m1_opacities_noalloc": (c_int, [P, P, P, P, P, P, P, c_int, c_int, P, ctypes.c_int64,
                                           P]),
     "bnsn_spectral_opacities": (c_int, [P, P, P, P, P, P, P, c_int, c_int, c_int, P,

@@ -161,6 +161,38 @@ def m1_opacities(eos, m1, flags, params, quad_1d, quad_2d=None, distr=None, stim
     return out
 
 
+def m1_opacities_grid_boxes(boxes, flags, params, quad_1d, quad_2d=None, in_scale=None,
+                            out_scale=None, stim_abs=1, precision="fp64", stream=None):
+    """Grey opacities of the interiors of grid boxes (bnsn_m1_opacities_grid_boxes).
+
+    boxes: dicts with "eos" [11, nz, ny, nx], "m1" [12, nz, ny, nx] and "out"
+    [20, nz, ny, nx] contiguous float64 CUDA tensors (a field per leading
+    index) and the interior "lo", "hi" as (i, j, k) index triples (x first).
+    in_scale (23) / out_scale (20): optional unit factors."""
+    arr = (C.GridBox * max(1, len(boxes)))()
+    for b, bx in enumerate(boxes):
+        eos, m1, out = bx["eos"], bx["m1"], bx["out"]
+        nz, ny, nx = eos.shape[1:]
+        for t, n_f in ((eos, 11), (m1, 12), (out, 20)):
+            if tuple(t.shape) != (n_f, nz, ny, nx) or not t.is_contiguous():
+                raise ValueError("box fields must be contiguous [fields, nz, ny, nx] tensors")
+        arr[b].shape[:] = [nx, ny, nz]
+        arr[b].lo[:] = [int(v) for v in bx["lo"]]
+        arr[b].hi[:] = [int(v) for v in bx["hi"]]
+        for f in range(11):
+            arr[b].eos[f] = _addr(eos, f)
+        for f in range(12):
+            arr[b].m1[f] = _addr(m1, f)
+        for f in range(20):
+            arr[b].out[f] = _addr(out, f)
+    q2 = quad_1d if quad_2d is None else quad_2d
+    sin = None if in_scale is None else (ctypes.c_double * 23)(*[float(v) for v in in_scale])
+    sout = None if out_scale is None else (ctypes.c_double * 20)(*[float(v) for v in out_scale])
+    _check(C.load().bnsn_m1_opacities_grid_boxes(
+        ctypes.byref(quad_1d), ctypes.byref(q2), ctypes.byref(flags), ctypes.byref(params), arr,
+        len(boxes), sin, sout, int(stim_abs), _prec(precision), _stream_handle(stream)))
+
+
 def spectral_opacities(eos, m1, flags, params, quad_1d, energies, distr=None, stimulated=1,
                        precision="fp64", out=None, stream=None):
     """Spectral opacities of N points at the given energies: [16, N, n_e]."""

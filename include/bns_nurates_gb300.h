@@ -286,6 +286,40 @@ int bnsn_m1_opacities(const MyQuadrature* quad_1d, const MyQuadrature* quad_2d,
                       const bnsn_m1_opacities_soa* out, int64_t npts,
                       void* stream);
 
+/* One box of a host code's 3-D grid (a THC / Cactus grid-function component,
+ * where the reference's exported headers -- utils/export_thc.py -- are called
+ * point by point inside the host code's loops): every field a separate device
+ * array of shape[0] x shape[1] x shape[2] doubles, x fastest.  The interior
+ * lo <= (i, j, k) < hi (ghost zones excluded) is evaluated; the rest of the
+ * output arrays is not touched.  Field order as in bnsn_eos_soa (mu_mu may
+ * be NULL), bnsn_m1_soa and bnsn_m1_opacities_soa. */
+typedef struct bnsn_grid_box
+{
+    int64_t shape[3];
+    int64_t lo[3];
+    int64_t hi[3];
+    const double* eos[11]; /* nb temp ye yp yn mu_p mu_n mu_e mu_mu dU dm_eff */
+    const double* m1[12];  /* n[4] J[4] chi[4] */
+    double* out[20];       /* eta_0[4] kappa_0_a[4] eta[4] kappa_a[4] kappa_s[4] */
+} bnsn_grid_box;
+
+/* Grey M1 opacities of the interiors of nboxes boxes (no counterpart in the
+ * reference, whose host codes loop over their grids calling
+ * ComputeM1Opacities per cell, m1_opacities.hpp:1172-1294): the interiors are
+ * gathered into one batch, evaluated as by bnsn_m1_opacities (distribution
+ * reconstructed from the M1 moments) and scattered back.  in_scale (23
+ * factors, eos then m1 fields) and out_scale (20) multiply the fields on the
+ * way in and out, converting the host code's units; NULL means 1.  Stream
+ * ordered; allocates a staging buffer of 43 doubles per interior cell from
+ * the device's default pool.  Invalid extents (lo > hi, hi > shape) and NULL
+ * field pointers of a non-empty box are rejected before any device work. */
+int bnsn_m1_opacities_grid_boxes(const MyQuadrature* quad_1d,
+                                 const MyQuadrature* quad_2d,
+                                 const OpacityFlags* flags, const OpacityParams* params,
+                                 const bnsn_grid_box* boxes, int nboxes,
+                                 const double* in_scale, const double* out_scale,
+                                 int stim_abs, int precision, void* stream);
+
 /* Grey M1 opacities without any device allocation (no counterpart in the
  * reference).  Same arguments and results as bnsn_m1_opacities, but the
  * per-point scratch records live in a static device array inside the library
