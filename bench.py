@@ -526,11 +526,21 @@ def run_blocks(args, rank, world, local):
         ms64 = timed("fp64", 1)
         fp64 = {"value": world * n / (ms64 * 1e-3), "unit": "points/s", "ms_per_step": ms64,
                 "steps": 1, "warmup": 1, "mixed_over_fp64": ms64 / ms}
-        r = rel_err(res, outs["fp64"].cpu().numpy())
+        r64 = outs["fp64"].cpu().numpy()
+        r = rel_err(res, r64)
         accuracy = {"vs": "plain FP64 GPU path (same plan, FP64), every output of every point",
                     "max_rel": float(r.max()), "p99_rel": float(np.percentile(r, 99)),
                     "p999_rel": float(np.percentile(r, 99.9)),
-                    "frac_above_1e-6": float(np.mean(r > 1e-6))}
+                    "frac_above_1e-6": float(np.mean(r > 1e-6)),
+                    **error_report(r, GREY_NAMES, degenerate_corner(eos_h))}
+
+        # conditioning: the FP64 plan's own change under +2 ulp of T or mu_e
+        # (where the reference's pair Psi formula is rounding noise, eta - s
+        # between ~35 and 200, the FP64 outputs move by orders of magnitude)
+        def grey64(e, o):
+            plans["fp64"].run(e, m1, o, stream=stream)
+
+        accuracy.update(conditioned_error(torch, eos, grey64, (20, n), r, r64, GREY_NAMES))
     # end to end: pinned host inputs -> device, graph replay, outputs -> host
     e2e = None
     if not args.no_e2e:

@@ -371,7 +371,9 @@ BNSN_DI void total_nu_f4(double omega, const Distr& d, bool same_cf, double* g)
 // Weak magnetism (weak_magnetism.hpp)
 // ---------------------------------------------------------------------------
 
-// weak_magnetism.hpp:45-104; reac 1: protons, 2: neutrons, 3: charged current
+// weak_magnetism.hpp:45-104; reac 1: protons, 2: neutrons, 3: charged current.
+// The four quotients by (1 + tau) share one reciprocal (FP64 division is a
+// multi-instruction sequence on the FP64 pipe; the results move by an ulp).
 BNSN_DI void nuc_form_factors(double E, int reac, double* cv, double* ca, double* F2)
 {
     const double lamp = 1.793, lamn = -1.913;
@@ -379,11 +381,11 @@ BNSN_DI void nuc_form_factors(double E, int reac, double* cv, double* ca, double
     const double tau  = 0.5 * (ehor * ehor) / (1. + ehor);
     const double eta  = 1. / (1. + 5.6 * tau);
     const double gq   = 1. + 4.97 * tau;
-    const double G    = 1. / (gq * gq);
-    const double Fp1  = (1. + tau * (1. + lamp)) * G / (1. + tau);
-    const double Fp2  = lamp * G / (1. + tau);
-    const double Fn1  = tau * lamn * (1. - eta) * G / (1. + tau);
-    const double Fn2  = lamn * (1. + tau * eta) * G / (1. + tau);
+    const double Gt   = 1. / ((gq * gq) * (1. + tau)); // G / (1 + tau)
+    const double Fp1  = (1. + tau * (1. + lamp)) * Gt;
+    const double Fp2  = lamp * Gt;
+    const double Fn1  = tau * lamn * (1. - eta) * Gt;
+    const double Fn2  = lamn * (1. + tau * eta) * Gt;
     const double d3   = 1. + 3.53 * tau;
     if (reac == 1)
     {
@@ -418,9 +420,9 @@ BNSN_DI void wm_abs_em(double omega, double* R, double* Rbar)
                         (8. / 3.) * cv * F2 * e2 +
                         (5. / 3.) * e2 * (1. + (2. / 5.) * e) * (F2 * F2);
     const double tmp2 = 4. * (cv + F2) * ca * e * (1. + (4. / 3.) * e);
-    const double tmp3 = ((k::Gv * k::Gv) + 3. * (k::Ga * k::Ga)) * (b * b * b);
-    *R    = (tmp1 + tmp2) / tmp3;
-    *Rbar = (tmp1 - tmp2) / tmp3;
+    const double itmp3 = 1. / (((k::Gv * k::Gv) + 3. * (k::Ga * k::Ga)) * (b * b * b));
+    *R    = (tmp1 + tmp2) * itmp3;
+    *Rbar = (tmp1 - tmp2) * itmp3;
 }
 
 // weak_magnetism.hpp:165-210
@@ -428,12 +430,14 @@ BNSN_DI void wm_scatt(double omega, int reac, double* R0, double* R1)
 {
     double cv, ca, F2;
     nuc_form_factors(omega, reac, &cv, &ca, &F2);
-    const double h0 = reac == 1 ? k::IsoH0p : k::IsoH0n;
-    const double h1 = reac == 1 ? k::IsoH1p : k::IsoH1n;
+    constexpr double ih0p = 1. / k::IsoH0p, ih0n = 1. / k::IsoH0n;
+    constexpr double ih1p = 1. / k::IsoH1p, ih1n = 1. / k::IsoH1n;
+    const double ih0 = reac == 1 ? ih0p : ih0n;
+    const double ih1 = reac == 1 ? ih1p : ih1n;
     const double e  = omega * k::WmEScale;
     const double ef = e * F2;
-    *R0 = ((cv * cv) + 3. * (ca * ca) + 1.5 * (ef * ef) + 2. * (e * e) * cv * F2) / h0;
-    *R1 = ((cv * cv) - (ca * ca) - 2. * (ef * ef) - 4. * (e * e) * cv * F2) / h1;
+    *R0 = ((cv * cv) + 3. * (ca * ca) + 1.5 * (ef * ef) + 2. * (e * e) * cv * F2) * ih0;
+    *R1 = ((cv * cv) - (ca * ca) - 2. * (ef * ef) - 4. * (e * e) * cv * F2) * ih1;
 }
 
 // ---------------------------------------------------------------------------
@@ -544,8 +548,9 @@ BNSN_DI double iso_scatt_total(double omega, double eta_pp, double eta_nn,
         wm_scatt(omega, 1, &R0p, &R1p);
         wm_scatt(omega, 2, &R0n, &R1n);
     }
-    const double pr = eta_pp * ((k::IsoC0p * R0p) - (k::IsoC1p * R1p) / 3.);
-    const double ne = eta_nn * ((k::IsoC0n * R0n) - (k::IsoC1n * R1n) / 3.);
+    constexpr double third = 1. / 3.;
+    const double pr = eta_pp * ((k::IsoC0p * R0p) - (k::IsoC1p * R1p) * third);
+    const double ne = eta_nn * ((k::IsoC0n * R0n) - (k::IsoC1n * R1n) * third);
     return pr + ne;
 }
 

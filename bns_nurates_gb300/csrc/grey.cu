@@ -220,6 +220,74 @@ __global__ void __launch_bounds__(128)
 // before the energy tables).
 constexpr int kHeadWords = (int)(offsetof(PointTab, nu) / sizeof(double));
 
+// TotalNuF of one species in FP32 with its exponent arguments in df form
+// (distribution.hpp:298-315): x rt - eta_t and P0 + c_f log x - x rf.  The
+// NES items take x = w = omega / T (rt = T / T_t, rf = T / T_f,
+// P0 = log beta_f + c_f log T), the prelude's beta and iso items x = omega
+// in MeV (rt = 1 / T_t, rf = 1 / T_f, P0 = log beta_f).  Both arguments cancel
+// (the product's leading part against eta_t or P0), so they are formed from
+// the exact FMA remainders; the occupation and its complement then keep FP32
+// relative accuracy (the complement from the two parts' complements,
+// w_t + w_f = 1 for the reconstructed distribution).
+struct NuSpecies
+{
+    dfm::df etat, rt, P0, cf, rf;
+    float wt, wf;
+};
+
+__device__ __forceinline__ void total_nu_one(dfm::df X, dfm::df LX, const NuSpecies& S,
+                                             float& g, float& gm)
+{
+    // a = x rt - eta_t as hi + lo; e^{-|a|} = e^{-|hi|} (1 -+ lo): a float
+    // exponent alone would cost |a| 6e-8 of relative accuracy
+    const dfm::df pa = dfm::two_prod(X.hi, S.rt.hi);
+    const dfm::df sa = dfm::two_sum(pa.hi, -S.etat.hi);
+    const dfm::df A  = dfm::fast_two_sum(
+        sa.hi, sa.lo + pa.lo + fmaf(X.hi, S.rt.lo, fmaf(X.lo, S.rt.hi, -S.etat.lo)));
+    const bool pos  = A.hi > 0.f;
+    const float t   = expf(-fabsf(A.hi)) * (pos ? 1.f - A.lo : 1.f + A.lo);
+    const float inv = nes32::rcp_nr(t + 1.f);
+    const float ft  = pos ? t * inv : inv;
+    const float ftm = pos ? inv : t * inv;
+    float fn        = 0.f;
+    if (S.wf != 0.f)
+    {
+        const dfm::df p1 = dfm::two_prod(S.cf.hi, LX.hi);
+        const dfm::df p2 = dfm::two_prod(-X.hi, S.rf.hi);
+        const dfm::df s1 = dfm::two_sum(S.P0.hi, p1.hi);
+        const dfm::df s2 = dfm::two_sum(s1.hi, p2.hi);
+        const float lo   = (S.P0.lo + p1.lo + p2.lo + s1.lo + s2.lo) +
+                         fmaf(S.cf.hi, LX.lo, S.cf.lo * LX.hi) - fmaf(X.hi, S.rf.lo, X.lo * S.rf.hi);
+        const dfm::df F = dfm::fast_two_sum(s2.hi, lo);
+        fn = expf(F.hi) * (1.f + F.lo);
+    }
+    g  = S.wt * ft + S.wf * fn;
+    gm = S.wt * ftm + S.wf * (1.f - fn);
+}
+
+// The constants of species s of distribution d for x = omega * xscale
+// (xscale = 1 / T for the NES items, 1 for omega in MeV); lxs = log xscale.
+__device__ __forceinline__ void nu_species(const Distr& d, int s, double xscale_inv, double lxs,
+                                           NuSpecies* S)
+{
+    S->wt   = (float)d.w_t[s];
+    S->wf   = (float)d.w_f[s];
+    S->etat = dfm::from_double(d.eta_t[s]);
+    S->rt   = dfm::from_double(xscale_inv / d.temp_t[s]);
+    const double lbf = d.beta_f[s] > 0. ? log(d.beta_f[s]) : 0.;
+    S->P0   = dfm::from_double(lbf - d.c_f[s] * lxs);
+    S->cf   = dfm::from_double(d.c_f[s]);
+    S->rf   = dfm::from_double(xscale_inv / d.temp_f[s]);
+}
+
+__device__ __forceinline__ void total_nu_q(dfm::df W, dfm::df LW, const NuSpecies* sp, float* g,
+                                           float* gm)
+{
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+        total_nu_one(W, LW, sp[s], g[s], gm[s]);
+}
+
 // ---------------------------------------------------------------------------
 // prelude
 // ---------------------------------------------------------------------------
@@ -227,18 +295,23 @@ __global__ void __launch_bounds__(kWarps * 32)
     grey_prelude_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
                         double* __restrict__ scratch)
 {
-    __shared__ double s_B1[kMaxM], s_x1[kMaxQ], s_x2[kMaxQ];
+    __shared__ double s_B1[kMaxM], s_x1[kMaxQ], s_x2[kMaxQ], s_lx1[kMaxQ];
     __shared__ PointTab s_tab[kWarps];
+    // mixed path: the occupation of the beta and iso items in FP32
+    // (total_nu_one), omega in MeV; the FP64 path keeps total_nu_f1
+    __shared__ NuSpecies s_nu[kWarps][4];
     for (int k = threadIdx.x; k < kMaxM; k += blockDim.x)
         s_B1[k] = L.B1[k];
     for (int k = threadIdx.x; k < kMaxQ; k += blockDim.x)
     {
-        s_x1[k] = L.x1[k];
-        s_x2[k] = L.x2[k];
+        s_x1[k]  = L.x1[k];
+        s_x2[k]  = L.x2[k];
+        s_lx1[k] = L.lx1[k];
     }
     __syncthreads();
     const int lane = threadIdx.x & 31;
     PointTab& W    = s_tab[threadIdx.x >> 5];
+    NuSpecies* Snu = s_nu[threadIdx.x >> 5];
     const int n1 = L.n1, n2 = L.n2, M = 2 * n2;
     const int64_t nwarp = (int64_t)gridDim.x * kWarps;
 
@@ -260,6 +333,8 @@ __global__ void __launch_bounds__(kWarps * 32)
             const double c0 = W.d.c_f[0];
             W.same_cf = ((W.d.c_f[1] == c0) && (W.d.c_f[2] == c0) && (W.d.c_f[3] == c0)) ? 1. : 0.;
         }
+        else if (L.mixed && lane >= 8 && lane < 12)
+            nu_species(W.d, lane - 8, 1., 0., &Snu[lane - 8]);
         __syncwarp();
         const bool same_cf = W.same_cf != 0.;
 
@@ -304,6 +379,7 @@ __global__ void __launch_bounds__(kWarps * 32)
             for (int kk = 0; kk < 8; ++kk)
                 acc[kk] = 0.;
             const int m1n = 2 * n1;
+            const double lsb0 = L.mixed ? log(sb[0]) : 0., lsb1 = L.mixed ? log(sb[1]) : 0.;
             for (int it = lane; it < 2 * m1n; it += 32)
             {
                 const int s = it >= m1n;
@@ -311,7 +387,16 @@ __global__ void __launch_bounds__(kWarps * 32)
                 const int i = a < n1 ? a : a - n1;
                 const double t  = sb[s];
                 const double nu = a < n1 ? t * s_x1[i] : t / s_x1[i];
-                const double g  = total_nu_f1(nu, W.d, s);
+                double g;
+                if (L.mixed)
+                {
+                    float gf, gmf;
+                    const double lnu = (s ? lsb1 : lsb0) + (a < n1 ? s_lx1[i] : -s_lx1[i]);
+                    total_nu_one(dfm::from_double(nu), dfm::from_double(lnu), Snu[s], gf, gmf);
+                    g = gf;
+                }
+                else
+                    g = total_nu_f1(nu, W.d, s);
                 double ab, em;
                 beta_rates(bp, nu, s, &ab, &em);
                 if (L.stim)
@@ -358,6 +443,13 @@ __global__ void __launch_bounds__(kWarps * 32)
                 s_iso[s] = (ns > k::ThresholdN) ? (L.m1[4 + s][p] / ns) : 1.5 * T;
             }
             double acc[4] = {0., 0., 0., 0.};
+            double lsi[4] = {0., 0., 0., 0.};
+            if (L.mixed)
+            {
+#pragma unroll
+                for (int s = 0; s < 4; ++s)
+                    lsi[s] = log(s_iso[s]);
+            }
             const int m1n = 2 * n1;
             for (int it = lane; it < 4 * m1n; it += 32)
             {
@@ -366,7 +458,17 @@ __global__ void __launch_bounds__(kWarps * 32)
                 const int i = a < n1 ? a : a - n1;
                 const double t   = s == 0 ? s_iso[0] : s == 1 ? s_iso[1] : s == 2 ? s_iso[2] : s_iso[3];
                 const double nu  = a < n1 ? t * s_x1[i] : t / s_x1[i];
-                const double g   = total_nu_f1(nu, W.d, s);
+                double g;
+                if (L.mixed)
+                {
+                    float gf, gmf;
+                    const double ls  = s == 0 ? lsi[0] : s == 1 ? lsi[1] : s == 2 ? lsi[2] : lsi[3];
+                    const double lnu = ls + (a < n1 ? s_lx1[i] : -s_lx1[i]);
+                    total_nu_one(dfm::from_double(nu), dfm::from_double(lnu), Snu[s], gf, gmf);
+                    g = gf;
+                }
+                else
+                    g = total_nu_f1(nu, W.d, s);
                 const double iso = iso_scatt_total(nu, W.eta_pp, W.eta_nn, L.use_WM_sc != 0);
                 const double aux = 4. * k::Pi * (nu * nu) * (nu * nu) * nu * iso;
                 const double v   = g * aux * s_B1[a];
@@ -508,17 +610,20 @@ __device__ __forceinline__ double cancel_factor_tot(const double* acc, const dou
     return amp;
 }
 
+// (element by element: the 16 warp sums are not held at once)
 __device__ __forceinline__ double cancel_factor(const double* acc, const float* mag, double scale,
                                                 double scale_e, const double* other)
 {
-    double a[16], m[16];
+    double amp = 1.;
 #pragma unroll
     for (int s = 0; s < 16; ++s)
     {
-        a[s] = warp_sum(acc[s]);
-        m[s] = warp_sum((double)mag[s]);
+        const double sc  = s < 8 ? scale : scale_e;
+        const double m   = warp_sum((double)mag[s]) * sc;
+        const double tot = fabs(warp_sum(acc[s]) * sc + other[s]);
+        amp = fmax(amp, m > 0. ? m / tot : 1.);
     }
-    return cancel_factor_tot(a, m, scale, scale_e, other);
+    return amp;
 }
 
 // v[0..16) summed over the CTA's NW warps in a fixed order; every thread
@@ -1735,15 +1840,6 @@ struct NesItem
     float pad;
 };
 
-// TotalNuF of one species with its exponent arguments in df form:
-// w rt - eta_t and P0 + c_f log w - w rf, rt = T/T_t, rf = T/T_f,
-// P0 = log beta_f + c_f log T (distribution.hpp:298-315).
-struct NuSpecies
-{
-    dfm::df etat, rt, P0, cf, rf;
-    float wt, wf;
-};
-
 // Per-warp data of the point in work.
 struct NesWarp
 {
@@ -1760,37 +1856,6 @@ struct NesSmem
     float2 dacc[16][kNesWarps * 32];  // per-lane df sums of the 16 moments
     float4 mag[4][kNesWarps * 32];    // per-lane sums of |term|
 };
-
-__device__ __forceinline__ void total_nu_q(dfm::df W, dfm::df LW, const NuSpecies* sp, float* g,
-                                           float* gm)
-{
-#pragma unroll
-    for (int s = 0; s < 4; ++s)
-    {
-        const NuSpecies& S = sp[s];
-        // the product's leading part and eta_t cancel inside one FMA
-        const float a =
-            fmaf(W.hi, S.rt.hi, -S.etat.hi) + fmaf(W.hi, S.rt.lo, fmaf(W.lo, S.rt.hi, -S.etat.lo));
-        const float t   = expf(-fabsf(a));
-        const float inv = nes32::rcp_nr(t + 1.f);
-        const float ft  = a > 0.f ? t * inv : inv;
-        const float ftm = a > 0.f ? inv : t * inv;
-        float fn        = 0.f;
-        if (S.wf != 0.f)
-        {
-            const dfm::df p1 = dfm::two_prod(S.cf.hi, LW.hi);
-            const dfm::df p2 = dfm::two_prod(-W.hi, S.rf.hi);
-            const dfm::df s1 = dfm::two_sum(S.P0.hi, p1.hi);
-            const dfm::df s2 = dfm::two_sum(s1.hi, p2.hi);
-            const float lo   = (S.P0.lo + p1.lo + p2.lo + s1.lo + s2.lo) +
-                             fmaf(S.cf.hi, LW.lo, S.cf.lo * LW.hi) -
-                             fmaf(W.hi, S.rf.lo, W.lo * S.rf.hi);
-            fn = expf(s2.hi + lo);
-        }
-        g[s]  = S.wt * ft + S.wf * fn;
-        gm[s] = S.wt * ftm + S.wf * (1.f - fn);
-    }
-}
 
 // Adds one item's terms to the lane's sums: em1..ab2 are R(nu, nubar) and
 // R(nubar, nu) with NEPSExpFunc applied, times (w w')^2 (m1_opacities.hpp:880-905).
@@ -1939,17 +2004,8 @@ __global__ void __launch_bounds__(kNesWarps * 32, 2)
                 Wd.lep[lane] = nes32::make_lepton(lane ? NP.eta1 : NP.eta0);
             else if (lane >= 8 && lane < 12)
             {
-                const int s    = lane - 8;
-                const Distr& d = Wd.N.d;
-                NuSpecies& Sp  = Wd.sp[s];
-                Sp.wt   = (float)d.w_t[s];
-                Sp.wf   = (float)d.w_f[s];
-                Sp.etat = dfm::from_double(d.eta_t[s]);
-                Sp.rt   = dfm::from_double(T / d.temp_t[s]);
-                const double lbf = d.beta_f[s] > 0. ? log(d.beta_f[s]) : 0.;
-                Sp.P0   = dfm::from_double(lbf + d.c_f[s] * log(T));
-                Sp.cf   = dfm::from_double(d.c_f[s]);
-                Sp.rf   = dfm::from_double(T / d.temp_f[s]);
+                // x = w = omega / T
+                nu_species(Wd.N.d, lane - 8, T, -log(T), &Wd.sp[lane - 8]);
             }
 #pragma unroll
             for (int kk = 0; kk < 16; ++kk)

@@ -18,6 +18,9 @@ HEADER = os.path.join(REPO, "include", "bns_nurates_gb300.h")
 
 def declared_functions():
     text = open(HEADER).read()
+    # declarations only: comments may name types or functions in prose
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", " ", text)
     return sorted(set(re.findall(r"\b(bnsn_[a-z0-9_]+)\s*\(", text)))
 
 
