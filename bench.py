@@ -578,7 +578,12 @@ def run_blocks(args, rank, world, local):
                              % (23 * 8 * n / 1e6),
                        "parallelism": f"{world} independent point shards"},
             "fp64_gpu": fp64, "accuracy": accuracy, "e2e": e2e,
-            "autotuner": {"plan_create_s": tune_s, "groups": groups},
+            "autotuner": {"plan_create_s": tune_s, "groups": groups,
+                          "layout": plans[args.precision].layout(),
+                          "knobs": "points per step (16k, 33k, 65k, 131k over all groups), "
+                                   "then persistent-grid scale (points per CTA, 4 or 2), each "
+                                   "timed on the first four steps of the data"},
+            "launches_per_replay": launches_per_step,
             "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps,
             "generator_s": gen_s,
         }

@@ -157,6 +157,8 @@ SIGNATURES = {
     "bnsn_blocks_run": (c_int, [P, P, P, P, P]),
     "bnsn_blocks_plan_groups": (c_int, [P]),
     "bnsn_blocks_plan_info": (c_int, [P, c_int, P, P, P, P, P, P]),
+    "bnsn_blocks_plan_layout": (c_int, [P, P, P, P]),
+    "bnsn_blocks_set_options": (c_int, [ctypes.c_int64, ctypes.c_int64]),
     "bnsn_blocks_plan_destroy": (c_int, [P]),
     "bnsn_fp64_peak_probe": (c_int, [ctypes.c_int64, P]),
     "bnsn_fp32_peak_probe": (c_int, [ctypes.c_int64, P]),

@@ -532,6 +532,20 @@ class BlocksPlan:
                             chunk=ch.value, grid_scale=gs.value))
         return res
 
+    def layout(self):
+        """Steps per run, points per step and scratch bytes of the plan."""
+        st, sp, nb = ctypes.c_int(), ctypes.c_int64(), ctypes.c_int64()
+        _check(C.load().bnsn_blocks_plan_layout(self._handle, ctypes.byref(st), ctypes.byref(sp),
+                                                ctypes.byref(nb)))
+        return dict(steps=st.value, step_points=sp.value, scratch_bytes=nb.value)
+
+    @staticmethod
+    def set_options(scratch_bytes=0, step_points=0):
+        """Options of plans created afterwards: the scratch limit in bytes (0:
+        a quarter of the free device memory) and the points per step over all
+        groups (0: the tuner's choice, or the default without tuning)."""
+        _check(C.load().bnsn_blocks_set_options(int(scratch_bytes), int(step_points)))
+
     def close(self):
         if self._handle:
             C.load().bnsn_blocks_plan_destroy(self._handle)

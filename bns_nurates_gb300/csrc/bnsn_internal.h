@@ -53,6 +53,20 @@ struct OpacityLaunch
     double* sout[16];      // j, kappa, j_s, kappa_s per species
 };
 
+// Multi-group launches of the batched AMR plan: one launch per phase serves
+// every configuration group, blockIdx.z selecting the group's descriptor and
+// its share of the chunk (points p0 .. p0 + np of its point list, scratch ws).
+struct GroupChunk
+{
+    int64_t p0, np;
+    double* ws;
+};
+struct GroupArgs
+{
+    const OpacityLaunch* Ls; // per group, device memory
+    const GroupChunk* gc;    // per group for the chunk of this launch, device memory
+};
+
 // Kernel phases of the timing hooks (bnsn_phase_times).
 enum Phase
 {
@@ -105,6 +119,14 @@ cudaError_t launch_grey(const OpacityLaunch& L, cudaStream_t stream, int num_sms
 // ws1.  The caller orders aux after stream0 before and joins it after.
 cudaError_t launch_grey_chunks(const OpacityLaunch& L, cudaStream_t stream0, cudaStream_t aux,
                                int num_sms, double* ws0, double* ws1, int64_t chunk, int64_t* k);
+// One multi-group step of the batched plan on `stream`: every phase kernel
+// launched once with grid z = groups; group z's descriptor is GA.Ls[z] and
+// its share of the step GA.gc[z] (both device memory).  U is a host
+// descriptor whose reaction flags are the union of the groups' (the phases
+// launched) and whose grid_scale sets the persistent grid; brem_set has bit i
+// set when a group uses brem variant i; np_max is the largest share.
+cudaError_t launch_grey_multi(const OpacityLaunch& U, unsigned brem_set, const GroupArgs& GA,
+                              unsigned groups, int64_t np_max, cudaStream_t stream, int num_sms);
 // Spectral opacities (phase kernels over chunks of points).  The scratch of
 // one call holds spectral_scratch_bytes(chunk, n_energies) bytes for chunks of
 // spectral_chunk_points(n_energies) points (about kSpecChunkRecords

@@ -162,10 +162,19 @@ __device__ __forceinline__ void beta_scales(double T, double eta_e, const double
 // ---------------------------------------------------------------------------
 constexpr int kPointTasks = 12;
 
+template <bool MULTI = false>
 __global__ void __launch_bounds__(128)
-    grey_point_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
-                      double* __restrict__ scratch)
+    grey_point_kernel(const __grid_constant__ OpacityLaunch L0, const GroupArgs GA, int64_t p0,
+                      int64_t np, double* __restrict__ scratch)
 {
+    const OpacityLaunch& L = MULTI ? GA.Ls[blockIdx.z] : L0;
+    if (MULTI)
+    {
+        const GroupChunk& gcz = GA.gc[blockIdx.z];
+        p0      = gcz.p0;
+        np      = gcz.np;
+        scratch = gcz.ws;
+    }
     const int task = blockIdx.y;
     if ((task >= 6 && task <= 9 && !(L.use_brem && L.brem_impl == 0)) ||
         (task == 10 && !(L.use_brem && L.brem_impl == 1)) || (task == 11 && !L.use_iso))
@@ -291,10 +300,19 @@ __device__ __forceinline__ void total_nu_q(dfm::df W, dfm::df LW, const NuSpecie
 // ---------------------------------------------------------------------------
 // prelude
 // ---------------------------------------------------------------------------
+template <bool MULTI = false>
 __global__ void __launch_bounds__(kWarps * 32)
-    grey_prelude_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
-                        double* __restrict__ scratch)
+    grey_prelude_kernel(const __grid_constant__ OpacityLaunch L0, const GroupArgs GA, int64_t p0,
+                        int64_t np, double* __restrict__ scratch)
 {
+    const OpacityLaunch& L = MULTI ? GA.Ls[blockIdx.z] : L0;
+    if (MULTI)
+    {
+        const GroupChunk& gcz = GA.gc[blockIdx.z];
+        p0      = gcz.p0;
+        np      = gcz.np;
+        scratch = gcz.ws;
+    }
     __shared__ double s_B1[kMaxM], s_x1[kMaxQ], s_x2[kMaxQ], s_lx1[kMaxQ];
     __shared__ PointTab s_tab[kWarps];
     // mixed path: the occupation of the beta and iso items in FP32
@@ -847,11 +865,21 @@ __device__ __forceinline__ void pair_kernel_q(const PairTab32& X, int a, int b, 
 // points the final kernel marked (predo), whose pair part of s2d it replaces;
 // that pass computes its Fermi-integral tables itself.  WIDE (that pass):
 // a point per CTA, its cells over all threads (the marked points are few).
-template <bool MIXED, bool WIDE = false>
+template <bool MIXED, bool WIDE = false, bool MULTI = false>
 __global__ void __launch_bounds__((WIDE ? 8 : kWarps) * 32)
-    grey_pair_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
-                     double* __restrict__ scratch, int redo_only)
+    grey_pair_kernel(const __grid_constant__ OpacityLaunch L0, const GroupArgs GA, int64_t p0,
+                     int64_t np, double* __restrict__ scratch, int redo_only)
 {
+    const OpacityLaunch& L = MULTI ? GA.Ls[blockIdx.z] : L0;
+    if (MULTI)
+    {
+        const GroupChunk& gcz = GA.gc[blockIdx.z];
+        p0      = gcz.p0;
+        np      = gcz.np;
+        scratch = gcz.ws;
+    }
+    if (MULTI && !L.use_pair)
+        return; // a group without pair (uniform over the CTA)
     constexpr int NW = WIDE ? 8 : kWarps;
     __shared__ double s_A1[kMaxM], s_A2[kMaxM];
     __shared__ uint32_t s_cells[kMaxCells];
@@ -1040,11 +1068,25 @@ struct Gp19Warp
 // IMPL: 0 HR98, 1 BRT06, 2 GP19.  ADD: accumulate onto the pair sums.
 // WIDE (the mixed path's FP64 pass over the few marked points): a point per
 // CTA, its cells over all threads.
-template <bool MIXED, int IMPL, bool WIDE = false>
+template <bool MIXED, int IMPL, bool WIDE = false, bool MULTI = false>
 __global__ void __launch_bounds__((WIDE ? 8 : kWarps) * 32)
-    grey_brem_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
-                     double* __restrict__ scratch, int add, int redo_only)
+    grey_brem_kernel(const __grid_constant__ OpacityLaunch L0, const GroupArgs GA, int64_t p0,
+                     int64_t np, double* __restrict__ scratch, int add, int redo_only)
 {
+    const OpacityLaunch& L = MULTI ? GA.Ls[blockIdx.z] : L0;
+    if (MULTI)
+    {
+        const GroupChunk& gcz = GA.gc[blockIdx.z];
+        p0      = gcz.p0;
+        np      = gcz.np;
+        scratch = gcz.ws;
+    }
+    if (MULTI)
+    {
+        if (!L.use_brem || L.brem_impl != IMPL)
+            return; // another brem variant's launch serves this group
+        add = L.use_pair;
+    }
     constexpr int NW = WIDE ? 8 : kWarps;
     constexpr int NT = WIDE ? 1 : kWarps; // point tables in flight per CTA
     __shared__ double s_A1[kMaxM], s_A2[kMaxM];
@@ -1566,11 +1608,21 @@ __host__ __device__ constexpr int nes_warps()
     return MODE == kNesFp64All ? kWarps : 8;
 }
 
-template <int MODE>
+template <int MODE, bool MULTI = false>
 __global__ void __launch_bounds__(nes_warps<MODE>() * 32, MODE == kNesAccurate ? 2 : 1)
-    grey_neps_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
-                     double* __restrict__ scratch)
+    grey_neps_kernel(const __grid_constant__ OpacityLaunch L0, const GroupArgs GA, int64_t p0,
+                     int64_t np, double* __restrict__ scratch)
 {
+    const OpacityLaunch& L = MULTI ? GA.Ls[blockIdx.z] : L0;
+    if (MULTI)
+    {
+        const GroupChunk& gcz = GA.gc[blockIdx.z];
+        p0      = gcz.p0;
+        np      = gcz.np;
+        scratch = gcz.ws;
+    }
+    if (MULTI && !L.use_inel)
+        return;
     constexpr bool MIX  = MODE == kNesAccurate;
     constexpr bool WIDE = MODE != kNesFp64All;  // a point per CTA
     constexpr int NW    = nes_warps<MODE>();
@@ -1913,10 +1965,21 @@ __device__ __forceinline__ void nes_accumulate(NesSmem& S, int t, bool stim, boo
     }
 }
 
+template <bool MULTI = false>
 __global__ void __launch_bounds__(kNesWarps * 32, 2)
-    grey_nes_fast_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
-                         double* __restrict__ scratch)
+    grey_nes_fast_kernel(const __grid_constant__ OpacityLaunch L0, const GroupArgs GA,
+                         int64_t p0, int64_t np, double* __restrict__ scratch)
 {
+    const OpacityLaunch& L = MULTI ? GA.Ls[blockIdx.z] : L0;
+    if (MULTI)
+    {
+        const GroupChunk& gcz = GA.gc[blockIdx.z];
+        p0      = gcz.p0;
+        np      = gcz.np;
+        scratch = gcz.ws;
+    }
+    if (MULTI && !L.use_inel)
+        return;
     extern __shared__ __align__(16) unsigned char nes_smem_raw[];
     NesSmem& S   = *reinterpret_cast<NesSmem*>(nes_smem_raw);
     const int n2 = L.n2, nn2 = n2 * n2, nit = 2 * nn2;
@@ -2183,10 +2246,19 @@ __global__ void __launch_bounds__(kNesWarps * 32, 2)
 // bad inputs, e.g. GP19 outside its table); read by grey_nonfinite_count.
 __device__ unsigned long long g_grey_nonfinite;
 
+template <bool MULTI = false>
 __global__ void __launch_bounds__(128)
-    grey_final_kernel(const __grid_constant__ OpacityLaunch L, int64_t p0, int64_t np,
-                      double* __restrict__ scratch, int redo_only)
+    grey_final_kernel(const __grid_constant__ OpacityLaunch L0, const GroupArgs GA, int64_t p0,
+                      int64_t np, double* __restrict__ scratch, int redo_only)
 {
+    const OpacityLaunch& L = MULTI ? GA.Ls[blockIdx.z] : L0;
+    if (MULTI)
+    {
+        const GroupChunk& gcz = GA.gc[blockIdx.z];
+        p0      = gcz.p0;
+        np      = gcz.np;
+        scratch = gcz.ws;
+    }
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < np;
          q += (int64_t)gridDim.x * blockDim.x)
     {
@@ -2286,8 +2358,8 @@ __global__ void __launch_bounds__(128)
                 nonfinite = nonfinite || !isfinite(o[qq]);
             }
         }
-        if (check)
-            P->bredo = bredo ? 1. : 0.;
+        if (!redo_only)
+            P->bredo = bredo ? 1. : 0.; // also where brem is off: scratch is reused
         if (check_pair)
             pair_mixed(P)->predo = predo ? 1. : 0.;
         if (!redo_only && L.mixed)
@@ -2320,70 +2392,189 @@ int grid_for(K kernel, int threads, int64_t work, int num_sms)
     return (int)(work < cap ? (work > 0 ? work : 1) : cap);
 }
 
+// One step of the phase pipeline.  Single launch (MULTI false): L is the
+// launch, points p0 .. p0 + np of it with scratch ws.  Multi-group launch: G
+// groups in grid z, their descriptors and chunk shares in GA (device memory);
+// L is a host copy whose flags are the union of the groups' (which phases
+// run), brem_set the brem variants present (bit i: variant i), np the largest
+// share (grid x), p0 and ws unused.
+struct Step
+{
+    OpacityLaunch const* L;
+    GroupArgs GA;
+    unsigned G;
+    unsigned brem_set;
+    int64_t p0, np;
+    double* ws;
+};
+
 // The fast NES pass: 8-warp CTAs with the item table and the per-lane sums in
 // dynamic shared memory (two CTAs per SM).
-cudaError_t launch_nes_fast(const OpacityLaunch& L, int64_t p0, int64_t np, double* ws,
-                            cudaStream_t st, int sms)
+template <bool MULTI>
+cudaError_t launch_nes_fast(const Step& S, cudaStream_t st, int sms)
 {
     const int smem    = (int)sizeof(NesSmem);
-    cudaError_t e     = cudaFuncSetAttribute(grey_nes_fast_kernel,
+    cudaError_t e     = cudaFuncSetAttribute(grey_nes_fast_kernel<MULTI>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess)
         return e;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grey_nes_fast_kernel,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grey_nes_fast_kernel<MULTI>,
                                                       kNesWarps * 32, smem) != cudaSuccess ||
         per_sm < 1)
         per_sm = 1;
-    const int64_t work = (np + kNesWarps - 1) / kNesWarps;
+    const int64_t work = (S.np + kNesWarps - 1) / kNesWarps;
     int64_t cap        = (int64_t)((double)sms * per_sm * g_grid_scale);
     cap                = cap < 1 ? 1 : cap;
     const int grid     = (int)(work < cap ? (work > 0 ? work : 1) : cap);
-    grey_nes_fast_kernel<<<grid, kNesWarps * 32, smem, st>>>(L, p0, np, ws);
+    grey_nes_fast_kernel<MULTI><<<dim3(grid, 1, MULTI ? S.G : 1), kNesWarps * 32, smem, st>>>(
+        *S.L, S.GA, S.p0, S.np, S.ws);
     return cudaGetLastError();
 }
 
-template <bool MIXED, int IMPL, bool WIDE>
-void launch_brem_impl(const OpacityLaunch& L, int64_t p0, int64_t np, double* ws,
-                      cudaStream_t st, int sms, int add, int redo_only)
+template <bool MIXED, int IMPL, bool WIDE, bool MULTI>
+void launch_brem_impl(const Step& S, cudaStream_t st, int sms, int add, int redo_only)
 {
     constexpr int threads = (WIDE ? 8 : kWarps) * 32;
-    const int64_t work    = WIDE ? np : (np + kWarps - 1) / kWarps;
-    grey_brem_kernel<MIXED, IMPL, WIDE>
-        <<<grid_for(grey_brem_kernel<MIXED, IMPL, WIDE>, threads, work, sms), threads, 0, st>>>(
-            L, p0, np, ws, add, redo_only);
+    const int64_t work    = WIDE ? S.np : (S.np + kWarps - 1) / kWarps;
+    const int gx          = grid_for(grey_brem_kernel<MIXED, IMPL, WIDE, MULTI>, threads, work, sms);
+    phase_mark(kPhBrem, 0, st);
+    grey_brem_kernel<MIXED, IMPL, WIDE, MULTI><<<dim3(gx, 1, MULTI ? S.G : 1), threads, 0, st>>>(
+        *S.L, S.GA, S.p0, S.np, S.ws, add, redo_only);
+    phase_mark(kPhBrem, 1, st);
+}
+
+template <bool MIXED, bool WIDE, bool MULTI>
+void launch_brem_set(const Step& S, cudaStream_t st, int sms, int add, int redo_only)
+{
+    // single launch: the launch's variant; multi-group: one launch per variant
+    // present (each returns at once for the other variants' groups)
+    const unsigned set = MULTI ? S.brem_set : 1u << S.L->brem_impl;
+    if (set & 1u)
+        launch_brem_impl<MIXED, 0, WIDE, MULTI>(S, st, sms, add, redo_only);
+    if (set & 2u)
+        launch_brem_impl<MIXED, 1, WIDE, MULTI>(S, st, sms, add, redo_only);
+    if (set & 4u)
+        launch_brem_impl<MIXED, 2, WIDE, MULTI>(S, st, sms, add, redo_only);
 }
 
 // redo_only (the FP64 pass over the points the final kernel marked) runs a
 // point per CTA.
-template <bool MIXED>
-cudaError_t launch_brem(const OpacityLaunch& L, int64_t p0, int64_t np, double* ws,
-                        cudaStream_t st, int sms, int add, int redo_only = 0)
+template <bool MIXED, bool MULTI>
+cudaError_t launch_brem(const Step& S, cudaStream_t st, int sms, int add, int redo_only = 0)
 {
-    phase_mark(kPhBrem, 0, st);
-    bool done = false;
     if constexpr (!MIXED)
     {
         if (redo_only)
+            launch_brem_set<false, true, MULTI>(S, st, sms, add, redo_only);
+        else
+            launch_brem_set<false, false, MULTI>(S, st, sms, add, redo_only);
+    }
+    else
+        launch_brem_set<true, false, MULTI>(S, st, sms, add, redo_only);
+    return cudaGetLastError();
+}
+
+// The phase kernels of one step on stream st: point constants, prelude, pair,
+// brem, NES, final, and on the mixed path the FP64 passes over the points the
+// final kernel marked, with a second final pass.
+template <bool MULTI>
+cudaError_t launch_step(const Step& S, cudaStream_t st, int sms)
+{
+    const OpacityLaunch& L = *S.L;
+    const int64_t np       = S.np;
+    const int64_t wb       = (np + kWarps - 1) / kWarps;
+    const unsigned gz      = MULTI ? S.G : 1;
+    cudaError_t err        = cudaSuccess;
+    phase_mark(kPhPrelude, 0, st);
+    {
+        const int64_t bx = (np + 127) / 128;
+        const dim3 pgrid((unsigned)(bx < (int64_t)sms * 4 ? bx : (int64_t)sms * 4), kPointTasks,
+                         gz);
+        grey_point_kernel<MULTI><<<pgrid, 128, 0, st>>>(L, S.GA, S.p0, np, S.ws);
+    }
+    phase_mark(kPhPrelude, 1, st);
+    phase_mark(kPhPrelude, 0, st);
+    grey_prelude_kernel<MULTI>
+        <<<dim3(grid_for(grey_prelude_kernel<MULTI>, kWarps * 32, wb, sms), 1, gz), kWarps * 32,
+           0, st>>>(L, S.GA, S.p0, np, S.ws);
+    phase_mark(kPhPrelude, 1, st);
+    if (L.use_pair)
+    {
+        phase_mark(kPhPair, 0, st);
+        if (L.mixed)
+            grey_pair_kernel<true, false, MULTI>
+                <<<dim3(grid_for(grey_pair_kernel<true, false, MULTI>, kWarps * 32, wb, sms), 1,
+                        gz),
+                   kWarps * 32, 0, st>>>(L, S.GA, S.p0, np, S.ws, 0);
+        else
+            grey_pair_kernel<false, false, MULTI>
+                <<<dim3(grid_for(grey_pair_kernel<false, false, MULTI>, kWarps * 32, wb, sms), 1,
+                        gz),
+                   kWarps * 32, 0, st>>>(L, S.GA, S.p0, np, S.ws, 0);
+        phase_mark(kPhPair, 1, st);
+    }
+    if (L.use_brem)
+    {
+        err = L.mixed ? launch_brem<true, MULTI>(S, st, sms, L.use_pair) :
+                        launch_brem<false, MULTI>(S, st, sms, L.use_pair);
+        if (err != cudaSuccess)
+            return err;
+    }
+    if (L.use_inel)
+    {
+        if (L.mixed)
         {
-            if (L.brem_impl == 0)
-                launch_brem_impl<false, 0, true>(L, p0, np, ws, st, sms, add, redo_only);
-            else if (L.brem_impl == 1)
-                launch_brem_impl<false, 1, true>(L, p0, np, ws, st, sms, add, redo_only);
-            else
-                launch_brem_impl<false, 2, true>(L, p0, np, ws, st, sms, add, redo_only);
-            done = true;
+            phase_mark(kPhNeps, 0, st);
+            if ((err = launch_nes_fast<MULTI>(S, st, sms)) != cudaSuccess)
+                return err;
+            phase_mark(kPhNeps, 1, st);
+            phase_mark(kPhNepsAccurate, 0, st);
+            constexpr int wa = nes_warps<kNesAccurate>() * 32;
+            grey_neps_kernel<kNesAccurate, MULTI>
+                <<<dim3(grid_for(grey_neps_kernel<kNesAccurate, MULTI>, wa, np, sms), 1, gz), wa,
+                   0, st>>>(L, S.GA, S.p0, np, S.ws);
+            phase_mark(kPhNepsAccurate, 1, st);
+            phase_mark(kPhNepsFp64, 0, st);
+            constexpr int wf = nes_warps<kNesFp64Flag>() * 32;
+            grey_neps_kernel<kNesFp64Flag, MULTI>
+                <<<dim3(grid_for(grey_neps_kernel<kNesFp64Flag, MULTI>, wf, np, sms), 1, gz), wf,
+                   0, st>>>(L, S.GA, S.p0, np, S.ws);
+            phase_mark(kPhNepsFp64, 1, st);
+        }
+        else
+        {
+            phase_mark(kPhNeps, 0, st);
+            grey_neps_kernel<kNesFp64All, MULTI>
+                <<<dim3(grid_for(grey_neps_kernel<kNesFp64All, MULTI>, kWarps * 32, wb, sms), 1,
+                        gz),
+                   kWarps * 32, 0, st>>>(L, S.GA, S.p0, np, S.ws);
+            phase_mark(kPhNeps, 1, st);
         }
     }
-    if (done)
-        ;
-    else if (L.brem_impl == 0)
-        launch_brem_impl<MIXED, 0, false>(L, p0, np, ws, st, sms, add, redo_only);
-    else if (L.brem_impl == 1)
-        launch_brem_impl<MIXED, 1, false>(L, p0, np, ws, st, sms, add, redo_only);
-    else
-        launch_brem_impl<MIXED, 2, false>(L, p0, np, ws, st, sms, add, redo_only);
-    phase_mark(kPhBrem, 1, st);
+    const dim3 fgrid(grid_for(grey_final_kernel<MULTI>, 128, (np + 127) / 128, sms), 1, gz);
+    phase_mark(kPhFinal, 0, st);
+    grey_final_kernel<MULTI><<<fgrid, 128, 0, st>>>(L, S.GA, S.p0, np, S.ws, 0);
+    phase_mark(kPhFinal, 1, st);
+    if (L.mixed && (L.use_brem || L.use_pair))
+    {
+        // points whose FP32 brem or pair sums the other reactions cancel:
+        // those parts in FP64, outputs again
+        if (L.use_pair)
+        {
+            phase_mark(kPhPair, 0, st);
+            grey_pair_kernel<false, true, MULTI>
+                <<<dim3(grid_for(grey_pair_kernel<false, true, MULTI>, 8 * 32, np, sms), 1, gz),
+                   8 * 32, 0, st>>>(L, S.GA, S.p0, np, S.ws, 1);
+            phase_mark(kPhPair, 1, st);
+        }
+        if (L.use_brem && (err = launch_brem<false, MULTI>(S, st, sms, L.use_pair, 1)) !=
+                              cudaSuccess)
+            return err;
+        phase_mark(kPhFinal, 0, st);
+        grey_final_kernel<MULTI><<<fgrid, 128, 0, st>>>(L, S.GA, S.p0, np, S.ws, 1);
+        phase_mark(kPhFinal, 1, st);
+    }
     return cudaGetLastError();
 }
 
@@ -2513,95 +2704,22 @@ cudaError_t launch_grey_chunks(const OpacityLaunch& L, cudaStream_t st0, cudaStr
         const cudaStream_t st = odd ? aux : st0;
         double* const wsk     = odd ? ws1 : ws0;
         const int64_t np      = (L.npts - p0) < chunk ? (L.npts - p0) : chunk;
-        const int64_t wb      = (np + kWarps - 1) / kWarps;
-        phase_mark(kPhPrelude, 0, st);
-        {
-            const int64_t bx = (np + 127) / 128;
-            const dim3 pgrid((unsigned)(bx < (int64_t)sms * 4 ? bx : (int64_t)sms * 4), kPointTasks);
-            grey_point_kernel<<<pgrid, 128, 0, st>>>(L, p0, np, wsk);
-        }
-        phase_mark(kPhPrelude, 1, st);
-        phase_mark(kPhPrelude, 0, st);
-        grey_prelude_kernel<<<grid_for(grey_prelude_kernel, kWarps * 32, wb, sms), kWarps * 32, 0,
-                              st>>>(L, p0, np, wsk);
-        phase_mark(kPhPrelude, 1, st);
-        if (L.use_pair)
-        {
-            phase_mark(kPhPair, 0, st);
-            if (L.mixed)
-                grey_pair_kernel<true><<<grid_for(grey_pair_kernel<true>, kWarps * 32, wb, sms),
-                                         kWarps * 32, 0, st>>>(L, p0, np, wsk, 0);
-            else
-                grey_pair_kernel<false><<<grid_for(grey_pair_kernel<false>, kWarps * 32, wb, sms),
-                                          kWarps * 32, 0, st>>>(L, p0, np, wsk, 0);
-            phase_mark(kPhPair, 1, st);
-        }
-        if (L.use_brem)
-        {
-            err = L.mixed ? launch_brem<true>(L, p0, np, wsk, st, sms, L.use_pair) :
-                            launch_brem<false>(L, p0, np, wsk, st, sms, L.use_pair);
-            if (err != cudaSuccess)
-                break;
-        }
-        if (L.use_inel)
-        {
-            if (L.mixed)
-            {
-                phase_mark(kPhNeps, 0, st);
-                if ((err = launch_nes_fast(L, p0, np, wsk, st, sms)) != cudaSuccess)
-                    break;
-                phase_mark(kPhNeps, 1, st);
-                phase_mark(kPhNepsAccurate, 0, st);
-                grey_neps_kernel<kNesAccurate>
-                    <<<grid_for(grey_neps_kernel<kNesAccurate>, nes_warps<kNesAccurate>() * 32, np,
-                                sms),
-                       nes_warps<kNesAccurate>() * 32,
-                       0, st>>>(L, p0, np, wsk);
-                phase_mark(kPhNepsAccurate, 1, st);
-                phase_mark(kPhNepsFp64, 0, st);
-                grey_neps_kernel<kNesFp64Flag>
-                    <<<grid_for(grey_neps_kernel<kNesFp64Flag>, nes_warps<kNesFp64Flag>() * 32, np,
-                                sms),
-                       nes_warps<kNesFp64Flag>() * 32,
-                       0, st>>>(L, p0, np, wsk);
-                phase_mark(kPhNepsFp64, 1, st);
-            }
-            else
-            {
-                phase_mark(kPhNeps, 0, st);
-                grey_neps_kernel<kNesFp64All>
-                    <<<grid_for(grey_neps_kernel<kNesFp64All>, kWarps * 32, wb, sms), kWarps * 32,
-                       0, st>>>(L, p0, np, wsk);
-                phase_mark(kPhNeps, 1, st);
-            }
-        }
-        phase_mark(kPhFinal, 0, st);
-        grey_final_kernel<<<grid_for(grey_final_kernel, 128, (np + 127) / 128, sms), 128, 0, st>>>(
-            L, p0, np, wsk, 0);
-        phase_mark(kPhFinal, 1, st);
-        if (L.mixed && (L.use_brem || L.use_pair))
-        {
-            // points whose FP32 brem or pair sums the other reactions cancel:
-            // those parts in FP64, outputs again
-            if (L.use_pair)
-            {
-                phase_mark(kPhPair, 0, st);
-                grey_pair_kernel<false, true>
-                    <<<grid_for(grey_pair_kernel<false, true>, 8 * 32, np, sms), 8 * 32, 0, st>>>(
-                        L, p0, np, wsk, 1);
-                phase_mark(kPhPair, 1, st);
-            }
-            if (L.use_brem &&
-                (err = launch_brem<false>(L, p0, np, wsk, st, sms, L.use_pair, 1)) != cudaSuccess)
-                break;
-            phase_mark(kPhFinal, 0, st);
-            grey_final_kernel<<<grid_for(grey_final_kernel, 128, (np + 127) / 128, sms), 128, 0,
-                                st>>>(L, p0, np, wsk, 1);
-            phase_mark(kPhFinal, 1, st);
-        }
-        err = cudaGetLastError();
+        const Step S          = {&L, GroupArgs{nullptr, nullptr}, 0u, 0u, p0, np, wsk};
+        err                   = launch_step<false>(S, st, sms);
     }
     return err;
+}
+
+cudaError_t launch_grey_multi(const OpacityLaunch& U, unsigned brem_set, const GroupArgs& GA,
+                              unsigned groups, int64_t np_max, cudaStream_t st, int sms)
+{
+    if (groups == 0 || np_max <= 0)
+        return cudaSuccess;
+    if (!GA.Ls || !GA.gc || groups > 65535u)
+        return cudaErrorInvalidValue;
+    g_grid_scale = U.grid_scale > 0. ? U.grid_scale : 4.;
+    const Step S = {&U, GA, groups, brem_set, 0, np_max, nullptr};
+    return launch_step<true>(S, st, sms);
 }
 
 cudaError_t launch_grey(const OpacityLaunch& L, cudaStream_t st0, int sms, double* ws,

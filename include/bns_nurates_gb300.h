@@ -371,29 +371,47 @@ typedef struct bnsn_block
 typedef struct bnsn_blocks_plan* bnsn_blocks_plan_t;
 
 /* Plan the blocks: group them by configuration, upload each group's point
- * list, allocate the per-point scratch, and with tune != 0 time candidate
- * launch shapes (points per scratch chunk, persistent-grid scale) per group on
- * the given arrays, keeping the fastest (the tuning runs write `out`).
- * Allocates device memory and synchronises; the GP19 table, when a block uses
- * it, must be loaded before and not replaced while the plan lives. */
+ * list and descriptor, split the points into steps (each step takes the same
+ * fraction of every group's points; steps alternate between two streams) and
+ * allocate the per-point scratch of two steps.  The step size is chosen by
+ * the tuner (tune != 0: candidate step sizes and persistent-grid scales --
+ * points per CTA -- timed on the first steps of the given arrays, keeping the
+ * fastest; the tuning runs write `out`), else a default or the size set by
+ * bnsn_blocks_set_options, with smaller steps where the scratch limit needs
+ * them.  Allocates device memory and synchronises; the GP19 table, when a
+ * block uses it, must be loaded before and not replaced while the plan
+ * lives. */
 int bnsn_blocks_plan_create(const bnsn_block* blocks, int nblocks,
                             const OpacityParams* params, int stim_abs, int precision,
                             int tune, const bnsn_eos_soa* eos, const bnsn_m1_soa* m1,
                             const bnsn_m1_opacities_soa* out, void* stream,
                             bnsn_blocks_plan_t* plan);
-/* Grey opacities of every block of the plan on `stream`.  Kernel launches
- * only (no allocation, host synchronisation or copy), so a run can be
- * captured in a CUDA graph and replayed; the arrays may differ from the ones
- * given to the plan but must hold the same points. */
+/* Grey opacities of every block of the plan on `stream`: per step, each phase
+ * kernel is launched once for all configuration groups.  Kernel launches only
+ * (no allocation, host synchronisation or copy), so a run can be captured in
+ * a CUDA graph and replayed; the arrays may differ from the ones given to the
+ * plan but must hold the same points.  Runs of one plan are ordered on the
+ * streams they are given: two runs of the same plan must not execute
+ * concurrently (they share the plan's scratch and descriptors). */
 int bnsn_blocks_run(bnsn_blocks_plan_t plan, const bnsn_eos_soa* eos,
                     const bnsn_m1_soa* m1, const bnsn_m1_opacities_soa* out,
                     void* stream);
-/* Number of configuration groups, and the configuration, size and chosen
- * launch shape of group g (reactions: bit 0 abs/em, 1 pair, 2 brem, 3 NES,
- * 4 iso).  Output pointers may be NULL. */
+/* Number of configuration groups, and the configuration, size and launch
+ * shape of group g (reactions: bit 0 abs/em, 1 pair, 2 brem, 3 NES, 4 iso;
+ * chunk: the group's points per step).  Output pointers may be NULL. */
 int bnsn_blocks_plan_groups(bnsn_blocks_plan_t plan);
 int bnsn_blocks_plan_info(bnsn_blocks_plan_t plan, int group, int* nquad, int* reactions,
                           int* brem, int64_t* npts, int64_t* chunk, double* grid_scale);
+/* The plan's steps per run, points per step (over all groups) and scratch
+ * bytes.  Output pointers may be NULL. */
+int bnsn_blocks_plan_layout(bnsn_blocks_plan_t plan, int* steps, int64_t* step_points,
+                            int64_t* scratch_bytes);
+/* Options of plans created afterwards (process-wide): scratch_bytes, the
+ * scratch limit (0: a quarter of the device memory free at plan creation; a
+ * plan holds at least two steps of one point per group); step_points, the
+ * points per step over all groups (0: the tuner's choice, or the default
+ * without tuning). */
+int bnsn_blocks_set_options(int64_t scratch_bytes, int64_t step_points);
 int bnsn_blocks_plan_destroy(bnsn_blocks_plan_t plan);
 
 /* Spectral opacities of npts points at n_energies neutrino energies
