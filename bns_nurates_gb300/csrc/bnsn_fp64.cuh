@@ -646,36 +646,6 @@ BNSN_DI void pair_kernel(double T, double eta, double omega, double omega_p,
         ab[s] = ex * em[s];
 }
 
-// The same kernel with one exponential: with E = e^{-s}, D = 1 - E, s = y + z,
-// 1/(1 - e^s) = -E/D and e^s/(1 - e^s) = -1/D, so
-// em = -(Phi T^2/2) A E/D and ab = -(Phi T^2/2) A / D (the reference's
-// clamped e^{+s} never appears).  s >= 2 y_min > 0.01 on the quadrature grids,
-// so D = 1 - E keeps a relative error below 1e-14; E itself is taken from exp,
-// never as 1 - D, which would lose every bit for large s.  Used by the mixed
-// path.
-BNSN_DI void pair_kernel_one_exp(double T, double eta, double y, double z, const double* fam,
-                                 const double* fap, const double* fbm, const double* fbp,
-                                 double f3e, double f4e, double* em, double* ab)
-{
-    double psi0, psi1;
-    pair_psi(eta, y, z, fam, fap, fbm, fbp, f3e, f4e, &psi0, &psi1);
-    const double s   = y + z;
-    const double ems = exp(-s); // e^{-s}
-    const double D   = 1. - ems;
-    const double K   = -0.5 * k::PairPhi * (T * T) / D;
-    const double a0  = (k::PairA1e * k::PairA1e) * psi0 + (k::PairA2e * k::PairA2e) * psi1;
-    const double a1  = (k::PairA1e * k::PairA1e) * psi1 + (k::PairA2e * k::PairA2e) * psi0;
-    const double a2  = (k::PairA1x * k::PairA1x) * psi0 + (k::PairA2x * k::PairA2x) * psi1;
-    const double a3  = (k::PairA1x * k::PairA1x) * psi1 + (k::PairA2x * k::PairA2x) * psi0;
-    ab[0] = K * a0;
-    ab[1] = K * a1;
-    ab[2] = K * a2;
-    ab[3] = K * a3;
-#pragma unroll
-    for (int q = 0; q < 4; ++q)
-        em[q] = ab[q] * ems;
-}
-
 // ---------------------------------------------------------------------------
 // HR98 bremsstrahlung (kernel_brem_HR98.hpp:33-393)
 // ---------------------------------------------------------------------------

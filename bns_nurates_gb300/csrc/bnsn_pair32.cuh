@@ -39,6 +39,7 @@
 
 #pragma once
 
+#include "bnsn_constants.h"
 #include "bnsn_df.cuh"
 
 namespace bnsn {
@@ -313,6 +314,38 @@ __device__ __forceinline__ bool make_cell(double y, double z, double eta, Cell& 
     const double s = y + z;
     lref = lcase == kLrefAbove ? s - eta : (lcase == kLrefBelow ? eta + s : 0.);
     return true;
+}
+
+// The pair kernel of one cell for the four species: em and ab of
+// kernel_pair.hpp:135-198 times (nu nubar)^2, from the FP32 integral:
+// ab = (Phi T^2 / 2) alpha . (Psi / (1 - e^s)) e^{s}, em = ab / SafeExp(s).
+// Y, Z: nu / T and nubar / T as double-float; eh = e^{y - |eta| / 2} and
+// dn = e^{-y} of each side (e^{Lref} = eh_y eh_z where Lref != 0, e^{-s} =
+// dn_y dn_z for s <= 700); sc = (Phi T^2 / 2) T^4 / 15, the point's factor.
+__device__ __forceinline__ void kernel_q(dfm::df Y, dfm::df Z, double ehy, double ehz,
+                                         double dny, double dnz, dfm::df ETA, double sc,
+                                         double* em, double* ab)
+{
+    Cell c;
+    int lcase;
+    if (!make_cell(Y, Z, ETA, c, lcase))
+    {
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            em[q] = ab[q] = 0.;
+        return;
+    }
+    double Q0, Q1;
+    cell_integrals(c, Q0, Q1);
+    const double f = lcase == kLrefZero ? sc : sc * (ehy * ehz);
+    ab[0] = f * ((k::PairA1e * k::PairA1e) * Q0 + (k::PairA2e * k::PairA2e) * Q1);
+    ab[1] = f * ((k::PairA1e * k::PairA1e) * Q1 + (k::PairA2e * k::PairA2e) * Q0);
+    ab[2] = f * ((k::PairA1x * k::PairA1x) * Q0 + (k::PairA2x * k::PairA2x) * Q1);
+    ab[3] = f * ((k::PairA1x * k::PairA1x) * Q1 + (k::PairA2x * k::PairA2x) * Q0);
+    const double ems = c.S.hi <= 700.f ? dny * dnz : 9.8596765437597708e-305; // e^-700
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        em[q] = ab[q] * ems;
 }
 
 } // namespace pair32

@@ -828,35 +828,13 @@ struct PairTab32
     double eh[kMaxM], dn[kMaxM];
 };
 
-// Pair cell (a, b) of the mixed path: Psi_0(y, z) and Psi_0(z, y) from the
-// cancellation-free FP32 integral (bnsn_pair32.cuh); em and ab of
-// kernel_pair.hpp:135-198 times (nu nubar)^2: ab = e^{s} em =
-// (Phi T^2 / 2) alpha . (Psi / (1 - e^s)) e^{s}, em = ab / SafeExp(s).
-// sc = (Phi T^2 / 2) T^4 / 15 (the point's factor).
+// Pair cell (a, b) of the mixed path from the per-warp node tables
+// (pair32::kernel_q).
 __device__ __forceinline__ void pair_kernel_q(const PairTab32& X, int a, int b, dfm::df ETA,
                                               double sc, double* em, double* ab)
 {
-    pair32::Cell c;
-    int lcase;
-    const dfm::df Ya = {X.yh[a], X.yl[a]}, Yb = {X.yh[b], X.yl[b]};
-    if (!pair32::make_cell(Ya, Yb, ETA, c, lcase))
-    {
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-            em[q] = ab[q] = 0.;
-        return;
-    }
-    double Q0, Q1;
-    pair32::cell_integrals(c, Q0, Q1);
-    const double f = lcase == pair32::kLrefZero ? sc : sc * (X.eh[a] * X.eh[b]);
-    ab[0] = f * ((k::PairA1e * k::PairA1e) * Q0 + (k::PairA2e * k::PairA2e) * Q1);
-    ab[1] = f * ((k::PairA1e * k::PairA1e) * Q1 + (k::PairA2e * k::PairA2e) * Q0);
-    ab[2] = f * ((k::PairA1x * k::PairA1x) * Q0 + (k::PairA2x * k::PairA2x) * Q1);
-    ab[3] = f * ((k::PairA1x * k::PairA1x) * Q1 + (k::PairA2x * k::PairA2x) * Q0);
-    const double ems = c.S.hi <= 700.f ? X.dn[a] * X.dn[b] : 9.8596765437597708e-305; // e^-700
-#pragma unroll
-    for (int q = 0; q < 4; ++q)
-        em[q] = ab[q] * ems;
+    pair32::kernel_q(dfm::df{X.yh[a], X.yl[a]}, dfm::df{X.yh[b], X.yl[b]}, X.eh[a], X.eh[b],
+                     X.dn[a], X.dn[b], ETA, sc, em, ab);
 }
 
 // MIXED: pair cells from the FP32 integral; the sums, their magnitudes and

@@ -21,15 +21,17 @@
 // per (output, node) (integration.hpp:524-543), which only repeats identical
 // values.
 //
-// MIXED: pb evaluates the brem kernel in FP32 (HR98 shape, GP19 profiles)
-// with the factor e^{-nu/T} of the emissivity applied in FP64 (BRT06 and the
-// GP19 high-T extrapolation stay FP64), and nes uses double-float Fermi
-// integrals and brackets with FP32 occupation factors formed as exponentials
-// of double-float arguments minus a per-energy scale (nes_spec_node), so
-// that e^{-(w - w')} g(w') stays in range at any nu/T; the pair kernel and
+// MIXED: pb evaluates the pair kernel as the cancellation-free FP32 integral
+// of the grey path (bnsn_pair32.cuh) and the brem kernel in FP32 (HR98
+// shape, GP19 profiles) with the factor e^{-nu/T} of the emissivity applied
+// in FP64 (BRT06 and the GP19 high-T extrapolation stay FP64), and nes uses
+// double-float Fermi integrals and brackets with FP32 occupation factors
+// formed as exponentials of double-float arguments minus a per-energy scale
+// (nes_spec_node), so that e^{-(w - w')} g(w') stays in range at any nu/T;
 // per-point data stay FP64 and every term is summed in FP64.  Both record an
 // error bound per output: the FP32 rounding bound (sum|t| over 1.25 for
-// brem, over 2 for NES) plus 1e9 x the components dropped below 2^-120.
+// brem, over 3 for the pair integrals, over 2 for NES) plus 1e9 x the
+// components dropped below 2^-120.
 // assemble compares the bounds with each output's total.  Where their sum
 // exceeds it (terms that cancel), or where a part could not run in FP32
 // (bound = inf: occupations outside the FP32 range, NES at nu/T < 0.05 where
@@ -47,6 +49,7 @@
 #include "bnsn_fp64.cuh"
 #include "bnsn_internal.h"
 #include "bnsn_mixed.cuh"
+#include "bnsn_pair32.cuh"
 
 namespace bnsn {
 namespace {
@@ -57,6 +60,10 @@ constexpr int kWarps  = 4;
 constexpr int kEChunk = 32; // energies staged per pass
 
 constexpr double kSpecCancelBrem = 1.25;    // sum|t| / |total| of the FP32 brem terms
+// same for the FP32 pair integrals: their terms are positive with <= 3e-7
+// relative error per cell (bnsn_pair32.cuh), so sum|t| / 3 is ~1e6 x the
+// error of their sum, the scale of the other bounds
+constexpr double kSpecCancelPair = 3.0;
 constexpr double kSpecCancelNes  = 2.0;     // same for the NES/NPS terms
 constexpr double kSpecCancelDf   = 1e5;     // same for the double-float NES pass
 constexpr double kSpecNesMinW    = 0.05;    // NES in FP64 below nu/T = 0.05
@@ -216,6 +223,8 @@ struct PbWarpMixed
     fp32::Hr98Mixed hm;
     float yeh[kEChunk], yel[kEChunk]; // nu / T as hi + lo
     float ybh[kMaxM], ybl[kMaxM];     // nubar / T as hi + lo
+    double ehy[kEChunk], dny[kEChunk]; // pair: e^{y - |eta|/2}, e^{-y} of the energies
+    double ehz[kMaxM], dnz[kMaxM];     // the same of the nodes
     float gb32[kMaxM][4], gbm32[kMaxM][4];
     float gp32[2][kGp19MaxW];
 };
@@ -344,6 +353,10 @@ __global__ void __launch_bounds__(kWarps * 32)
         }
         __syncwarp();
         const bool same_cf = W.same_cf != 0;
+        // mixed pair: eta and the point's factor (Phi T^2 / 2) T^4 / 15
+        const dfm::df ETA = dfm::from_double(eta_e);
+        const double T2   = T * T;
+        const double scq  = 0.5 * k::PairPhi * T2 * (T2 * T2) / 15.;
         // antineutrino grid of the pair/brem integral (m1_opacities.hpp:1542)
         const double ts = k::TempMultiple * T;
         for (int a = lane; a < M; a += 32)
@@ -358,6 +371,11 @@ __global__ void __launch_bounds__(kWarps * 32)
                 const dfm::df yd = dfm::from_double(nu / T);
                 X.ybh[a] = yd.hi;
                 X.ybl[a] = yd.lo;
+                if (L.use_pair)
+                {
+                    X.ehz[a] = exp(W.zb[a] - 0.5 * fabs(eta_e));
+                    X.dnz[a] = exp(-W.zb[a]);
+                }
 #pragma unroll
                 for (int s = 0; s < 4; ++s)
                 {
@@ -366,7 +384,9 @@ __global__ void __launch_bounds__(kWarps * 32)
                 }
             }
         }
-        if (L.use_pair)
+        // the FP64 pair kernel's Fermi integrals (the mixed pass uses the
+        // FP32 integral, bnsn_pair32.cuh)
+        if (L.use_pair && !MIX)
             for (int t = lane; t < 2 * M; t += 32)
             {
                 const int a    = t >> 1;
@@ -412,7 +432,7 @@ __global__ void __launch_bounds__(kWarps * 32)
                 if (!((cm >> c) & 1u))
                     continue;
                 const double y = L.energies[e0 + c] / T;
-                if (L.use_pair && !skip)
+                if (L.use_pair && !skip && !MIX)
                 {
                     fdi_orders<1, 5>(eta_e - y, W.fmy[c]);
                     fdi_orders<1, 5>(eta_e + y, W.fpy[c]);
@@ -422,6 +442,11 @@ __global__ void __launch_bounds__(kWarps * 32)
                     const dfm::df yd = dfm::from_double(y);
                     X.yeh[c] = yd.hi;
                     X.yel[c] = yd.lo;
+                    if (L.use_pair)
+                    {
+                        X.ehy[c] = exp(y - 0.5 * fabs(eta_e));
+                        X.dny[c] = exp(-y);
+                    }
                 }
             }
             __syncwarp();
@@ -438,10 +463,15 @@ __global__ void __launch_bounds__(kWarps * 32)
                 for (int kk = 0; kk < 8; ++kk)
                     acc[kk] = 0.;
                 float gl[8]; // mixed: sum|t| / 1.25 + 1e9 x dropped
+                double gp[8]; // mixed: sum|t| of the FP32 pair terms
 #pragma unroll
                 for (int kk = 0; kk < 8; ++kk)
+                {
                     gl[kk] = 0.f;
+                    gp[kk] = 0.;
+                }
                 const double sbe = sb * exp(-w); // brem emission carries e^{-nu/T}
+                const double inu2 = MIX ? 1. / (nu * nu) : 0.;
                 if (act && !skip)
                 {
                     for (int a = grp; a < M; a += Gq)
@@ -451,15 +481,9 @@ __global__ void __launch_bounds__(kWarps * 32)
                         const double* gb = W.gb[a];
                         double pe[4] = {0., 0., 0., 0.}, pa[4] = {0., 0., 0., 0.};
                         double be = 0., ba = 0.;
-                        if (L.use_pair)
-                        {
-                            if (MIX) // one exponential, no division by T
-                                pair_kernel_one_exp(T, eta_e, w, W.zb[a], W.fmy[c], W.fpy[c],
-                                                    W.fmz[a], W.fpz[a], W.fe3, W.fe4, pe, pa);
-                            else
-                                pair_kernel(T, eta_e, nu, nub, w, W.zb[a], W.fmy[c], W.fpy[c],
-                                            W.fmz[a], W.fpz[a], W.fe3, W.fe4, pe, pa);
-                        }
+                        if (L.use_pair && !MIX)
+                            pair_kernel(T, eta_e, nu, nub, w, W.zb[a], W.fmy[c], W.fpy[c],
+                                        W.fmz[a], W.fpz[a], W.fe3, W.fe4, pe, pa);
                         if (L.use_brem && !b32)
                         {
                             if (L.brem_impl == 0)
@@ -473,13 +497,37 @@ __global__ void __launch_bounds__(kWarps * 32)
                                 gp19_kernel(G19, nbar, ye, T, nu, nub, &be, &ba);
                         }
                         const double nb2 = nub * nub;
-#pragma unroll
-                        for (int s = 0; s < 4; ++s)
+                        if (!MIX || (L.use_brem && !b32))
                         {
-                            const int ps    = s ^ 1;
-                            const double bf = nbb ? 1. : 1. - gb[ps];
-                            acc[s] += wa * (nb2 * ((pe[s] + be) * bf));
-                            acc[4 + s] += wa * (nb2 * ((pa[s] + ba) * gb[ps]));
+#pragma unroll
+                            for (int s = 0; s < 4; ++s)
+                            {
+                                const int ps    = s ^ 1;
+                                const double bf = nbb ? 1. : 1. - gb[ps];
+                                acc[s] += wa * (nb2 * ((pe[s] + be) * bf));
+                                acc[4 + s] += wa * (nb2 * ((pa[s] + ba) * gb[ps]));
+                            }
+                        }
+                        if (MIX && L.use_pair)
+                        {
+                            // FP32 pair integral: (em, ab) (nu nubar)^2, positive
+                            double qe[4], qa[4];
+                            pair32::kernel_q(dfm::df{X.yeh[c], X.yel[c]},
+                                             dfm::df{X.ybh[a], X.ybl[a]}, X.ehy[c], X.ehz[a],
+                                             X.dny[c], X.dnz[a], ETA, scq, qe, qa);
+                            const double wq = wa * inu2;
+#pragma unroll
+                            for (int s = 0; s < 4; ++s)
+                            {
+                                const int ps    = s ^ 1;
+                                const double bf = nbb ? 1. : 1. - gb[ps];
+                                const double te = wq * (qe[s] * bf);
+                                const double ta = wq * (qa[s] * gb[ps]);
+                                acc[s] += te;
+                                acc[4 + s] += ta;
+                                gp[s] += fabs(te);
+                                gp[4 + s] += fabs(ta);
+                            }
                         }
                         if (MIX && b32)
                         {
@@ -561,7 +609,11 @@ __global__ void __launch_bounds__(kWarps * 32)
                 {
                     acc[kk] = seg_sum(acc[kk], Gq);
                     if (MIX)
+                    {
                         gl[kk] = seg_sum(gl[kk], Gq);
+                        if (L.use_pair)
+                            gp[kk] = seg_sum(gp[kk], Gq);
+                    }
                 }
                 if (act && grp == 0)
                 {
@@ -574,7 +626,8 @@ __global__ void __launch_bounds__(kWarps * 32)
                             E.bpb[kk] = skip ? INFINITY
                                              : (b32 ? (kk < 4 ? sbe : sb) *
                                                           ((double)gl[kk] + kSpecFloor)
-                                                    : 0.);
+                                                    : 0.) +
+                                                   gp[kk] * (1. / kSpecCancelPair);
                         else if (MODE == kSpecRedo)
                             E.bpb[kk] = 0.;
                     }
