@@ -30,7 +30,7 @@
 // (nes_spec_node), so that e^{-(w - w')} g(w') stays in range at any nu/T;
 // per-point data stay FP64 and every term is summed in FP64.  Both record an
 // error bound per output: the FP32 rounding bound (sum|t| over 1.25 for
-// brem, over 3 for the pair integrals, over 2 for NES) plus 1e9 x the
+// brem, over 2.5 for the pair integrals, over 2 for NES) plus 1e9 x the
 // components dropped below 2^-120.
 // assemble compares the bounds with each output's total.  Where their sum
 // exceeds it (terms that cancel), or where a part could not run in FP32
@@ -60,10 +60,10 @@ constexpr int kWarps  = 4;
 constexpr int kEChunk = 32; // energies staged per pass
 
 constexpr double kSpecCancelBrem = 1.25;    // sum|t| / |total| of the FP32 brem terms
-// same for the FP32 pair integrals: their terms are positive with <= 3e-7
-// relative error per cell (bnsn_pair32.cuh), so sum|t| / 3 is ~1e6 x the
-// error of their sum, the scale of the other bounds
-constexpr double kSpecCancelPair = 3.0;
+// same for the FP32 pair integrals: their terms are positive with at most
+// 4.1e-7 relative error per cell (bnsn_pair32.cuh), so sum|t| / 2.5 is 1e6 x
+// a bound on the error of their sum, the scale of the other bounds
+constexpr double kSpecCancelPair = 2.5;
 constexpr double kSpecCancelNes  = 2.0;     // same for the NES/NPS terms
 constexpr double kSpecCancelDf   = 1e5;     // same for the double-float NES pass
 constexpr double kSpecNesMinW    = 0.05;    // NES in FP64 below nu/T = 0.05
