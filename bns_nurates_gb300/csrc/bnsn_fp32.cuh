@@ -135,6 +135,33 @@ BNSN_DI float hr98_shape(const Hr98Mixed& M, float xh_in, float xl_in)
     return tot;
 }
 
+// K_1(x) e^{x} for x > 0 (the BRT06 brem kernel's Bessel factor with its
+// detailed-balance exponential folded in): the polynomial approximations of
+// Abramowitz & Stegun 9.8.3, 9.8.7 and 9.8.8 that the FP64 bessk1 uses
+// (functions.hpp:99-180), evaluated in FP32; e^{x} multiplies K_1 for
+// x <= 2 and cancels the e^{-x} of the large-x form otherwise, so the result
+// stays O(x^{-1/2}) at any x.
+BNSN_DI float bessk1e(float x)
+{
+    if (x <= 2.f)
+    {
+        const float t  = x * (1.f / 3.75f);
+        const float u  = t * t;
+        const float i1 = x * (0.5f + u * (0.87890594f + u * (0.51498869f + u * (0.15084934f +
+                         u * (0.2658733e-1f + u * (0.301532e-2f + u * 0.32411e-3f))))));
+        const float y  = 0.25f * (x * x);
+        const float k1 = logf(0.5f * x) * i1 +
+                         (1.f / x) * (1.f + y * (0.15443144f + y * (-0.67278579f +
+                         y * (-0.18156897f + y * (-0.1919402e-1f + y * (-0.110404e-2f +
+                         y * (-0.4686e-4f)))))));
+        return k1 * expf(x);
+    }
+    const float y = 2.f / x;
+    return (1.25331414f + y * (0.23498619f + y * (-0.3655620e-1f + y * (0.1504268e-1f +
+            y * (-0.780353e-2f + y * (0.325614e-2f + y * (-0.68245e-3f))))))) /
+           sqrtf(x);
+}
+
 #undef BNSN_DI
 
 } // namespace fp32

@@ -1172,11 +1172,12 @@ __global__ void __launch_bounds__((WIDE ? 8 : kWarps) * 32)
             else
                 __syncwarp();
         }
-        // Mixed cells in FP32 except BRT06, the GP19 high-T extrapolation and
-        // points whose pair sums are negative somewhere: there the outputs
-        // (pair + brem + ...) cancel and would magnify FP32 rounding.
+        // Mixed cells in FP32 except the GP19 high-T extrapolation (which
+        // differences two table values); points whose cells the other
+        // reactions cancel go to FP64 below (the guard).
         const bool fp32_cells =
-            MIXED && (IMPL == 0 || (IMPL == 2 && prof && GW.pt.regime != 3 && GW.pt.regime != 5));
+            MIXED && (IMPL == 0 || IMPL == 1 ||
+                      (IMPL == 2 && prof && GW.pt.regime != 3 && GW.pt.regime != 5));
         double acc[16], bm[16];
 #pragma unroll
         for (int kk = 0; kk < 16; ++kk)
@@ -1191,6 +1192,8 @@ __global__ void __launch_bounds__((WIDE ? 8 : kWarps) * 32)
             float thr = 0.f, lt2 = 0.f;
             if (IMPL == 0)
                 scale *= C.hm.outer;
+            else if (IMPL == 1)
+                scale *= C.brt06_pre;
             else
             {
                 scale *= 3. * GW.pt.C;
@@ -1214,6 +1217,13 @@ __global__ void __launch_bounds__((WIDE ? 8 : kWarps) * 32)
                 bool slow = false;
                 if (IMPL == 0)
                     Kab = fp32::hr98_shape(C.hm, xs.hi, xs.lo);
+                else if (IMPL == 1)
+                {
+                    // BRT06 (kernel_brem_BRT06.hpp:24-69): ab = pre K_1(x) e^{x} / x,
+                    // x = (nu_a + nu_b) / 2T; em = ab e^{-2x}
+                    const float xh = 0.5f * (xs.hi + xs.lo);
+                    Kab            = fp32::bessk1e(xh) / xh;
+                }
                 else
                 {
                     double wv = C.nu[a] + C.nu[b];
