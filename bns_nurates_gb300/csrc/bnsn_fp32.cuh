@@ -162,6 +162,36 @@ BNSN_DI float bessk1e(float x)
            sqrtf(x);
 }
 
+// The iso-energetic scattering kernel's weak-magnetism factor of one nucleon
+// (reac 1: protons, 2: neutrons) in FP32: (C0 R0 - C1 R1 / 3) / IsoConst of
+// formulas_beta_iso.hpp:411-507 with R0, R1 of weak_magnetism.hpp:165-210 and
+// the form factors of weak_magnetism.hpp:45-104.  All its terms are positive
+// (cv F2 >= 0 for both nucleons), so FP32 keeps ~1e-7; 1 - 1/(1 + 5.6 tau) is
+// formed as 5.6 tau / (1 + 5.6 tau), without the cancellation at small tau.
+BNSN_DI float iso_wm_factor(float omega, int reac)
+{
+    constexpr float lamp = 1.793f, lamn = -1.913f;
+    constexpr float cw   = (float)(0.5 - 2. * k::SinThW2);
+    const float e    = omega * (float)k::WmEScale;
+    const float tau  = 0.5f * (e * e) / (1.f + e);
+    const float eta  = 1.f / (1.f + 5.6f * tau);
+    const float gq   = 1.f + 4.97f * tau;
+    const float Gt   = 1.f / ((gq * gq) * (1.f + tau));
+    const float Fp1  = (1.f + tau * (1.f + lamp)) * Gt;
+    const float Fp2  = lamp * Gt;
+    const float Fn1  = tau * lamn * (5.6f * tau * eta) * Gt;
+    const float Fn2  = lamn * (1.f + tau * eta) * Gt;
+    const float d3   = 1.f + 3.53f * tau;
+    const float cv   = reac == 1 ? cw * Fp1 - 0.5f * Fn1 : cw * Fn1 - 0.5f * Fp1;
+    const float ca   = (reac == 1 ? 0.5f * (float)(k::Ga - k::Gs) : -0.5f * (float)(k::Ga + k::Gs)) /
+                     (d3 * d3);
+    const float F2   = reac == 1 ? cw * Fp2 - 0.5f * Fn2 : cw * Fn2 - 0.5f * Fp2;
+    const float ef   = e * F2;
+    const float A0   = (cv * cv) + 3.f * (ca * ca) + 1.5f * (ef * ef) + 2.f * (e * e) * cv * F2;
+    const float A1   = (cv * cv) - (ca * ca) - 2.f * (ef * ef) - 4.f * (e * e) * cv * F2;
+    return A0 - A1 * (1.f / 3.f);
+}
+
 #undef BNSN_DI
 
 } // namespace fp32

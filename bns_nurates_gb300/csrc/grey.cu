@@ -487,7 +487,13 @@ __global__ void __launch_bounds__(kWarps * 32)
                 }
                 else
                     g = total_nu_f1(nu, W.d, s);
-                const double iso = iso_scatt_total(nu, W.eta_pp, W.eta_nn, L.use_WM_sc != 0);
+                // mixed: the weak-magnetism factors in FP32 (positive terms; the
+                // iso sum enters kappa_s alone, no other reaction cancels it)
+                const double iso =
+                    (L.mixed && L.use_WM_sc)
+                        ? k::IsoConst * (W.eta_pp * (double)fp32::iso_wm_factor((float)nu, 1) +
+                                         W.eta_nn * (double)fp32::iso_wm_factor((float)nu, 2))
+                        : iso_scatt_total(nu, W.eta_pp, W.eta_nn, L.use_WM_sc != 0);
                 const double aux = 4. * k::Pi * (nu * nu) * (nu * nu) * nu * iso;
                 const double v   = g * aux * s_B1[a];
                 if (s == 0) acc[0] += v;
