@@ -44,6 +44,20 @@ def test_blocks_plan_argument_errors(lib):
     assert lib.bnsn_blocks_run(None, None, None, None, None) == C.ERR_ARG
 
 
+def test_blocks_options_and_layout_argument_errors(lib):
+    """bnsn_blocks_set_options rejects negative values and keeps the last
+    valid options; bnsn_blocks_plan_layout rejects a NULL plan (no device
+    work in either)."""
+    assert lib.bnsn_blocks_set_options(-1, 0) == C.ERR_ARG
+    assert lib.bnsn_blocks_set_options(0, -5) == C.ERR_ARG
+    assert lib.bnsn_blocks_set_options(1 << 30, 4096) == C.OK
+    assert lib.bnsn_blocks_set_options(0, 0) == C.OK
+    steps = ctypes.c_int(-7)
+    assert lib.bnsn_blocks_plan_layout(None, ctypes.byref(steps), None, None) == C.ERR_ARG
+    assert steps.value == -7
+    assert lib.bnsn_blocks_plan_groups(None) == 0
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_blocks_match_direct_calls(cuda, precision):
